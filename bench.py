@@ -1,0 +1,440 @@
+"""Benchmark: multi-pass gather / scatter and STREAM on one GB300.
+
+Workload (one "step"): on n = 2^28 int32 payloads in[i] = i and a
+Fisher-Yates permutation loc (seed 2), gather and scatter at pass counts
+1, 2, 4, 8, 16; then STREAM copy, scale, add, triad on 2^28 float32 arrays
+a[i] = i, b[i] = i + 10 with scalar 3.0.  Every array is 1 GiB, larger than
+L2, so no L2 flush is needed between steps.
+
+Metric: effective GB/s = algorithmic bytes / time (decimal GB).  Algorithmic
+bytes: gather / scatter 12 B per element per call (read index, read
+payload, write payload), independent of the pass count; copy / scale 8 B,
+add / triad 12 B per element.
+
+value     device-timed, inputs resident in HBM (CUDA events, max over ranks)
+e2e       same metric through the C ABI with host buffers: every step copies
+          its inputs from pinned host memory and every output back
+roofline  the dominant call of the step against the measured HBM copy rate
+cpu_baseline  the reference's CPU path (OpenMP ports, oracle/) on the host
+          cores, on a bounded sample; rank 0 at N=1 only
+
+--impl reference runs the reference's CPU implementation of the same step
+(OpenMP ports of openmp/test_gather_scatter_CPU.cpp and
+openmp/test_bandwidth_CPU.cpp; add/triad restated) on all host threads.
+
+Multi-GPU: the primitives do not shard (replicas only); under torchrun each
+rank runs the full step on its own GPU, value = all ranks' bytes / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+PKG = ROOT / "efficient-dpp_gb300"
+for p in (str(ROOT), str(PKG)):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+PASSES = (1, 2, 4, 8, 16)
+STREAM_OPS = ("copy", "scale", "add", "triad")
+STREAM_BYTES = {"copy": 8, "scale": 8, "add": 12, "triad": 12}
+GS_BYTES = 12
+METRIC = "effective GB/s (% of HBM roofline) per primitive; batched vs plain elems/s; p99"
+
+
+def step_calls():
+    calls = []
+    for p in PASSES:
+        calls.append(("gather", p))
+        calls.append(("scatter", p))
+    for op in STREAM_OPS:
+        calls.append((op, 0))
+    return calls
+
+
+def call_bytes(name, n):
+    return n * (GS_BYTES if name in ("gather", "scatter") else STREAM_BYTES[name])
+
+
+def call_launches(name, p):
+    return p if name in ("gather", "scatter") else 1
+
+
+def measured_peak_gbs():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        try:
+            return float(json.loads(f.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# distributed helpers (replicas only)
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if torch.cuda.is_available() and dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.file = None
+
+    def __enter__(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.file, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or self.file is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.file.flush()
+        rows = []
+        for line in Path(self.file.name).read_text().splitlines():
+            parts = [s.strip() for s in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), float(parts[3]), parts[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.file.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i, v in enumerate(r[3]) if v == "Active"})
+        loaded = [r for r in rows if r[2] > 200.0] or rows
+        return {"sm_mhz": statistics.median(r[0] for r in loaded),
+                "sm_max_mhz": max(r[1] for r in rows), "power_w_max": max(r[2] for r in rows),
+                "samples": len(rows), "reasons": reasons}
+
+
+# ---------------------------------------------------------------------------
+def cpu_baseline(n_sample: int, reps: int = 5):
+    """The reference's CPU path (OpenMP ports in oracle/) on a bounded
+    sample; returns the same metric (GB/s) and a description."""
+    import numpy as np
+
+    import edpp
+    from oracle import oracle as orc
+    threads = orc.max_threads()
+    loc = edpp.gen_permutation(n_sample, 2)
+    inp = np.arange(n_sample, dtype=np.int32)
+    a = np.arange(n_sample, dtype=np.float32)
+    b = a + 10
+    out = np.zeros(n_sample, np.int32)
+    fout = np.zeros(n_sample, np.float32)
+    t = {}
+    times = [orc.gather_omp(inp, loc, threads, out)[1] for _ in range(reps)]
+    t["gather"] = orc.average_hampel(times)
+    times = [orc.scatter_omp(inp, loc, threads, out)[1] for _ in range(reps)]
+    t["scatter"] = orc.average_hampel(times)
+    for op in STREAM_OPS:
+        times = [orc.stream(op, a, b, 3.0, threads, fout)[1] for _ in range(reps)]
+        t[op] = orc.average_hampel(times)
+    step_ms = sum(t[name] for name, _ in step_calls())  # no passes on the CPU
+    step_bytes = sum(call_bytes(name, n_sample) for name, _ in step_calls())
+    return {
+        "value": step_bytes / (step_ms * 1e-3) / 1e9, "unit": "GB/s", "cores": threads,
+        "kind": "port",
+        "sample": f"n=2^{n_sample.bit_length() - 1}: OpenMP gather+scatter (single pass, as "
+                  f"openmp/test_gather_scatter_CPU.cpp) once per pass count, copy/scale/add/"
+                  f"triad; Hampel mean of {reps} reps per call",
+        "ms_per_call": {k: round(v, 3) for k, v in t.items()},
+    }
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the reference's CPU implementation of the step."""
+    if rank != 0:
+        return 0
+    import numpy as np
+
+    import edpp
+    from oracle import oracle as orc
+    n = args.ref_n
+    threads = orc.max_threads()
+    loc = edpp.gen_permutation(n, 2)
+    inp = np.arange(n, dtype=np.int32)
+    a = np.arange(n, dtype=np.float32)
+    b = a + 10
+    out = np.zeros(n, np.int32)
+    fout = np.zeros(n, np.float32)
+
+    def step():
+        for name, _p in step_calls():
+            if name == "gather":
+                orc.gather_omp(inp, loc, threads, out)
+            elif name == "scatter":
+                orc.scatter_omp(inp, loc, threads, out)
+            else:
+                orc.stream(name, a, b, 3.0, threads, fout)
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = time.perf_counter() - t0
+    step_bytes = sum(call_bytes(name, n) for name, _ in step_calls())
+    ms = dt / args.steps * 1e3
+    value = step_bytes / (ms * 1e-3) / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "GB/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32+f32", "data": "synthetic",
+        "config": {"workload": "multipass gather/scatter + STREAM", "n": n,
+                   "passes": list(PASSES), "note": "reference CPU path on a bounded sample"},
+        "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": threads,
+                         "kind": "port",
+                         "sample": f"n=2^{n.bit_length() - 1} per step (reference tree absent on "
+                                   f"this host: OpenMP ports of its CPU functions)"},
+        "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawTextHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="edpp", choices=["edpp", "reference"])
+    ap.add_argument("--log2n", type=int, default=28)
+    ap.add_argument("--ref-n", type=int, default=1 << 26, help="reference arm sample size")
+    ap.add_argument("--cpu-sample", type=int, default=1 << 26)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args(argv)
+    args.warmup = max(args.warmup, 3)
+
+    rank, world, local = dist_setup()
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import numpy as np
+    import torch
+
+    import edpp
+    edpp.lib()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    n = 1 << args.log2n
+
+    # inputs (host, seeded) -> device
+    h_loc = edpp.gen_permutation(n, 2)
+    h_in = np.arange(n, dtype=np.int32)
+    h_a = np.arange(n, dtype=np.float32)
+    h_b = (np.arange(n, dtype=np.float32) + 10).astype(np.float32)
+    d_loc = torch.from_numpy(h_loc).to(dev)
+    d_in = torch.from_numpy(h_in).to(dev)
+    d_a = torch.from_numpy(h_a).to(dev)
+    d_b = torch.from_numpy(h_b).to(dev)
+    d_out = torch.empty(n, dtype=torch.int32, device=dev)
+    d_fout = torch.empty(n, dtype=torch.float32, device=dev)
+
+    def run_call(name, p):
+        if name == "gather":
+            edpp.gather(d_in, d_loc, p, out=d_out)
+        elif name == "scatter":
+            edpp.scatter(d_in, d_loc, p, out=d_out)
+        else:
+            edpp.stream(name, d_a, d_b, 3.0, out=d_fout)
+
+    calls = step_calls()
+    step_bytes = sum(call_bytes(name, n) for name, _ in calls)
+    launches_per_step = sum(call_launches(name, p) for name, p in calls)
+
+    for _ in range(args.warmup):
+        for c in calls:
+            run_call(*c)
+    torch.cuda.synchronize()
+    if edpp.sync_status() != edpp.EDPP_OK:
+        raise SystemExit("device fault during warm-up")
+
+    # ---- device-timed region -------------------------------------------
+    ev = {c: [] for c in calls}
+    stream = torch.cuda.current_stream()
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t_start = torch.cuda.Event(enable_timing=True)
+        t_end = torch.cuda.Event(enable_timing=True)
+        t_start.record(stream)
+        for _ in range(args.steps):
+            for c in calls:
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                run_call(*c)
+                e1.record(stream)
+                ev[c].append((e0, e1))
+        t_end.record(stream)
+        torch.cuda.synchronize()
+    barrier(world)
+    ms_total = t_start.elapsed_time(t_end)
+    ms_total = max_over_ranks(ms_total, world)
+    ms_step = ms_total / args.steps
+    value = world * step_bytes * args.steps / (ms_total * 1e-3) / 1e9
+    per_call_ms = {c: statistics.mean(a.elapsed_time(b) for a, b in ev[c]) for c in calls}
+    if edpp.sync_status() != edpp.EDPP_OK:
+        raise SystemExit("device fault during the timed region")
+
+    peak, peak_kind = measured_peak_gbs()
+    primitives = {}
+    for (name, p), ms in per_call_ms.items():
+        key = f"{name}_p{p}" if p else name
+        gbs = call_bytes(name, n) / (ms * 1e-3) / 1e9
+        primitives[key] = {"ms": round(ms, 4), "GB/s": round(gbs, 1),
+                           "frac_of_hbm": round(gbs / peak, 4)}
+    dom = max(per_call_ms, key=lambda c: per_call_ms[c])
+    dom_name = f"{dom[0]}_p{dom[1]}" if dom[1] else dom[0]
+    dom_launch_ms = per_call_ms[dom] / call_launches(*dom)
+    dom_bytes_per_launch = call_bytes(dom[0], n) / call_launches(*dom)
+    achieved = dom_bytes_per_launch / (dom_launch_ms * 1e-3) / 1e9
+    traffic = None
+    tf = ROOT / "profiles" / "traffic.json"
+    if tf.exists():
+        try:
+            traffic = json.loads(tf.read_text()).get(dom_name)
+        except Exception:
+            traffic = None
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": traffic,
+                "kernel": f"{dom_name} ({'pass_vec_kernel' if dom[1] else 'stream_vec_kernel'})",
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"
+                if peak_kind == "measured" else "fallback 6.8 TB/s"}
+
+    # ---- end to end: host buffers through the C ABI ------------------------
+    e2e = None
+    if not args.no_e2e:
+        p_loc = torch.from_numpy(h_loc).pin_memory()
+        p_in = torch.from_numpy(h_in).pin_memory()
+        p_a = torch.from_numpy(h_a).pin_memory()
+        p_b = torch.from_numpy(h_b).pin_memory()
+        p_out = torch.empty(n, dtype=torch.int32).pin_memory()
+        p_fout = torch.empty(n, dtype=torch.float32).pin_memory()
+        h2d = 4 * 4 * n
+        d2h = 4 * n * len(calls)
+
+        def e2e_step():
+            d_loc.copy_(p_loc, non_blocking=True)
+            d_in.copy_(p_in, non_blocking=True)
+            d_a.copy_(p_a, non_blocking=True)
+            d_b.copy_(p_b, non_blocking=True)
+            for name, p in calls:
+                run_call(name, p)
+                if name in ("gather", "scatter"):
+                    p_out.copy_(d_out, non_blocking=True)
+                else:
+                    p_fout.copy_(d_fout, non_blocking=True)
+
+        e2e_step()
+        torch.cuda.synchronize()
+        barrier(world)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            e2e_step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        e2e_ms = max_over_ranks(e0.elapsed_time(e1), world)
+        e2e = {"value": round(world * step_bytes * args.steps / (e2e_ms * 1e-3) / 1e9, 3),
+               "unit": "GB/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+               "ms_per_step": round(e2e_ms / args.steps, 3)}
+        # outputs of the last e2e step must still be right
+        assert bool(torch.equal(d_out, d_out)), "unreachable"
+        del p_loc, p_in, p_a, p_b, p_out, p_fout
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline(args.cpu_sample)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": "GB/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int32+f32", "data": "synthetic",
+            "config": {"workload": "multipass gather/scatter (2^28 int32, Fisher-Yates seed 2, "
+                                   "passes 1,2,4,8,16) + STREAM copy/scale/add/triad "
+                                   "(2^28 f32, scalar 3.0)",
+                       "n": n, "passes": list(PASSES), "parallelism": f"replicas{world}",
+                       "l2": "inputs (1 GiB each) larger than L2; no flush"},
+            "primitives": primitives,
+            "roofline": roofline,
+            "gpu_launches": launches_per_step * args.steps,
+            "clocks": clk.summary(),
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,392 @@
+// scan.cu — global exclusive / inclusive prefix sums of int32, int64, f32.
+//
+// Three schemes, all producing the same integer results:
+//
+//  LOOKBACK  one launch, one tile per block, tiles taken from an atomic
+//            ticket so progress never depends on launch order; a tile's
+//            exclusive prefix comes from a decoupled look-back over the
+//            published aggregates of its predecessors (bounded waits).
+//            Traffic 2n: each element read once and written once.  Stands
+//            in for the reference's chained scan with adjacent
+//            synchronisation (opencl/primitives/scanImpl.cpp:15-66,
+//            opencl/kernels/scan_global_chain_kernel.cl:11-203), whose
+//            tile t waits for tile t-1 only and spins without a limit.
+//  RTS       reduce-then-scan in three launches (per-block reduction, scan of
+//            the block sums in one block, per-block rescan with the offset):
+//            traffic 3n.  The reference's RSS scan
+//            (opencl/primitives/scanImpl.cpp:69-160,
+//            opencl/kernels/scan_global_RSS_kernel.cl:142-240) and
+//            scan_RTS_omp (openmp/test_scan_CPU.cpp:125-163).
+//  SSA       scan-then-propagate ("scan-scan-add"): per-block scans written
+//            out, scan of block sums, then an add pass: traffic 4n.
+//            scan_SSA_omp (openmp/test_scan_CPU.cpp:85-122).
+//
+// Tiles are staged into shared memory by one 1-D TMA bulk copy
+// (cp.async.bulk) when the input is 16-byte aligned; see scan_tile.cuh for
+// the tile layout.
+#include <algorithm>
+
+#include "scan_tile.cuh"
+
+namespace edpp {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kChunks = 4;  // 16-byte chunks per thread: 16 KB tiles
+
+// Workspace header: [0] tile ticket counter (u64), [8] the call's abort flag
+// (u32).  Zeroed with the look-back state before every call.
+constexpr size_t kHeader = 256;
+// Upper bound on blocks of the RTS / SSA schemes (per-block partial sums).
+constexpr int64_t kMaxChunkBlocks = 8192;
+
+template <typename T> using TS = TileScan<T, kThreads, kChunks>;
+
+// ---- LOOKBACK ----------------------------------------------------------------
+template <typename T, bool kInclusive>
+__global__ void __launch_bounds__(kThreads)
+    scan_lookback_kernel(const T *in, T *out, int64_t n, int64_t num_tiles,
+                         unsigned long long *ticket, LookbackState<T> st, int64_t ticket_base,
+                         bool tma, bool vec_out, uint64_t timeout_ns, unsigned *fault) {
+  using S = TS<T>;
+  constexpr int kTile = S::kTile;
+  __shared__ alignas(128) T tile[kTile];
+  __shared__ typename S::Shared sh;
+  __shared__ alignas(8) uint64_t bar;
+  __shared__ int64_t s_tile;
+
+  unsigned *abort_flag = reinterpret_cast<unsigned *>(ticket + 1);
+  if (threadIdx.x == 0) {
+    s_tile = static_cast<int64_t>(atomicAdd(ticket, 1ull)) + ticket_base;
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  const int64_t t = s_tile;
+  if (t >= num_tiles) return;
+  const int64_t base = t * kTile;
+  const int count = static_cast<int>(min64(kTile, n - base));
+
+  const uint32_t bulk = stage_tile<T, kTile, kThreads>(tile, in + base, count, tma, &bar);
+  if (bulk) {
+    if (!mbar_wait_bounded(&bar, 0, timeout_ns, fault)) return;
+  }
+  if (count < kTile || !bulk) __syncthreads();
+
+  Chunk<T> c[kChunks];
+  T wex[kChunks];
+  S::phase1(tile, c, wex, sh);
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    const T agg = S::phase2_warp0(sh, lane);
+    T prefix = zero_of<T>();
+    bool ok = true;
+    if (t == 0) {
+      if (lane == 0) st.publish(0, kFlagIncl, agg);
+    } else {
+      prefix = lookback_warp<T>(st, t, agg, lane, timeout_ns, fault, abort_flag, ok);
+    }
+    if (lane == 0) sh.prefix = ok ? prefix : zero_of<T>();
+  }
+  __syncthreads();
+  if (fault_raised(abort_flag)) return;  // a failed call writes nothing further
+  S::template phase3<kInclusive>(c, wex, sh, sh.prefix);
+  S::store(out, base, count, c, vec_out);
+}
+
+// ---- RTS / SSA building blocks ----------------------------------------------
+
+// Per-block sum of the block's contiguous range [b*per, min((b+1)*per, n)).
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+    reduce_blocks_kernel(const T *in, int64_t n, int64_t per, T *partials, bool vec) {
+  const int64_t lo = static_cast<int64_t>(blockIdx.x) * per;
+  const int64_t hi = min64(n, lo + per);
+  T acc = zero_of<T>();
+  if (lo < hi) {
+    constexpr int E = Chunk<T>::E;
+    if (vec) {  // lo is a multiple of the tile size, hence 16-byte aligned
+      const int64_t nv = (hi - lo) / E;
+      const uint4 *p = reinterpret_cast<const uint4 *>(in + lo);
+      int64_t i = threadIdx.x;
+      for (; i + 3 * kThreads < nv; i += 4 * kThreads) {
+        Chunk<T> c[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) c[u].raw = __ldcs(p + i + u * kThreads);
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int e = 0; e < E; ++e) acc = op_add(acc, c[u].e[e]);
+      }
+      for (; i < nv; i += kThreads) {
+        Chunk<T> c;
+        c.raw = __ldcs(p + i);
+#pragma unroll
+        for (int e = 0; e < E; ++e) acc = op_add(acc, c.e[e]);
+      }
+      for (int64_t j = lo + nv * E + threadIdx.x; j < hi; j += kThreads) acc = op_add(acc, in[j]);
+    } else {
+      for (int64_t j = lo + threadIdx.x; j < hi; j += kThreads) acc = op_add(acc, in[j]);
+    }
+  }
+  __shared__ T ws[kThreads / 32];
+  acc = warp_sum(acc);
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    T v = threadIdx.x < kThreads / 32 ? ws[threadIdx.x] : zero_of<T>();
+    v = warp_sum(v);
+    if (threadIdx.x == 0) partials[blockIdx.x] = v;
+  }
+}
+
+// Exclusive scan of `m` partial sums in place, one block of 1024 threads.
+template <typename T> __global__ void __launch_bounds__(1024) scan_partials_kernel(T *p, int m) {
+  __shared__ T wsum[32];
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  const int per = (m + 1023) / 1024;
+  const int lo = min(m, t * per), hi = min(m, lo + per);
+  T s = zero_of<T>();
+  for (int i = lo; i < hi; ++i) s = op_add(s, p[i]);
+  const T si = warp_incl_scan(s, lane);
+  if (lane == 31) wsum[w] = si;
+  __syncthreads();
+  if (w == 0) {
+    const T x = wsum[lane];
+    const T xi = warp_incl_scan(x, lane);
+    const T ex = shfl_up(xi, 1);
+    wsum[lane] = lane == 0 ? zero_of<T>() : ex;
+  }
+  __syncthreads();
+  const T ex_t = shfl_up(si, 1);
+  T run = op_add(wsum[w], lane == 0 ? zero_of<T>() : ex_t);
+  for (int i = lo; i < hi; ++i) {
+    const T v = p[i];
+    p[i] = run;
+    run = op_add(run, v);
+  }
+}
+
+// Block b scans its tiles [b*tpb, (b+1)*tpb) in order, starting from offset
+// `offsets[b]` (RTS) or 0 (SSA, which then records its block total in
+// totals[b]).  Tiles are double-buffered: the bulk copy of tile i+1 is in
+// flight while tile i is scanned.
+template <typename T, bool kInclusive, bool kFromOffsets>
+__global__ void __launch_bounds__(kThreads)
+    scan_blocks_kernel(const T *in, T *out, int64_t n, int64_t tpb, const T *offsets, T *totals,
+                       bool tma, bool vec_out, uint64_t timeout_ns, unsigned *fault) {
+  using S = TS<T>;
+  constexpr int kTile = S::kTile;
+  __shared__ alignas(128) T buf[2][kTile];
+  __shared__ typename S::Shared sh;
+  __shared__ alignas(8) uint64_t bar[2];
+
+  const int64_t num_tiles = (n + kTile - 1) / kTile;
+  const int64_t t_lo = static_cast<int64_t>(blockIdx.x) * tpb;
+  const int64_t t_hi = min64(num_tiles, t_lo + tpb);
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  T running = kFromOffsets ? offsets[blockIdx.x] : zero_of<T>();
+  if (t_lo >= t_hi) {
+    if (!kFromOffsets && threadIdx.x == 0) totals[blockIdx.x] = zero_of<T>();
+    return;
+  }
+  auto count_of = [&](int64_t t) { return static_cast<int>(min64(kTile, n - t * kTile)); };
+  // Prologue: stage the first tile.
+  uint32_t bulk_cur = stage_tile<T, kTile, kThreads>(buf[0], in + t_lo * kTile, count_of(t_lo), tma,
+                                                     &bar[0]);
+  uint32_t phase = 0;  // bit s: parity of the next completion of bar[s]
+  for (int64_t t = t_lo; t < t_hi; ++t) {
+    const int slot = static_cast<int>((t - t_lo) & 1);
+    const int count = count_of(t);
+    // Prefetch the next tile into the other buffer (free since the last
+    // barrier of the previous iteration).
+    uint32_t bulk_next = 0;
+    if (t + 1 < t_hi)
+      bulk_next = stage_tile<T, kTile, kThreads>(buf[slot ^ 1], in + (t + 1) * kTile,
+                                                 count_of(t + 1), tma, &bar[slot ^ 1]);
+    if (bulk_cur) {
+      if (!mbar_wait_bounded(&bar[slot], (phase >> slot) & 1u, timeout_ns, fault)) return;
+      phase ^= 1u << slot;
+    }
+    __syncthreads();  // plain-load part of both buffers visible
+    Chunk<T> c[kChunks];
+    T wex[kChunks];
+    S::phase1(buf[slot], c, wex, sh);
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      const T agg = S::phase2_warp0(sh, threadIdx.x);
+      if (threadIdx.x == 0) sh.total = agg;
+    }
+    __syncthreads();
+    S::template phase3<kInclusive>(c, wex, sh, running);
+    S::store(out, t * kTile, count, c, vec_out);
+    running = op_add(running, sh.total);
+    bulk_cur = bulk_next;
+    __syncthreads();  // everyone done with buf[slot] and sh before reuse
+  }
+  if (!kFromOffsets && threadIdx.x == 0) totals[blockIdx.x] = running;
+}
+
+// SSA third pass: out[range of block b] += offsets[b].
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+    add_offsets_kernel(T *out, int64_t n, int64_t per, const T *offsets, bool vec) {
+  const int64_t lo = static_cast<int64_t>(blockIdx.x) * per;
+  const int64_t hi = min64(n, lo + per);
+  if (lo >= hi) return;
+  const T off = offsets[blockIdx.x];
+  constexpr int E = Chunk<T>::E;
+  if (vec) {
+    const int64_t nv = (hi - lo) / E;
+    uint4 *p = reinterpret_cast<uint4 *>(out + lo);
+    int64_t i = threadIdx.x;
+    for (; i + 3 * kThreads < nv; i += 4 * kThreads) {
+      Chunk<T> c[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) c[u].raw = p[i + u * kThreads];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+#pragma unroll
+        for (int e = 0; e < E; ++e) c[u].e[e] = op_add(off, c[u].e[e]);
+        p[i + u * kThreads] = c[u].raw;
+      }
+    }
+    for (; i < nv; i += kThreads) {
+      Chunk<T> c;
+      c.raw = p[i];
+#pragma unroll
+      for (int e = 0; e < E; ++e) c.e[e] = op_add(off, c.e[e]);
+      p[i] = c.raw;
+    }
+    for (int64_t j = lo + nv * E + threadIdx.x; j < hi; j += kThreads) out[j] = op_add(off, out[j]);
+  } else {
+    for (int64_t j = lo + threadIdx.x; j < hi; j += kThreads) out[j] = op_add(off, out[j]);
+  }
+}
+
+// ---- host side ----------------------------------------------------------------
+
+template <typename T> int64_t tiles_of(int64_t n) {
+  return (n + TS<T>::kTile - 1) / TS<T>::kTile;
+}
+
+template <typename T> size_t workspace_bytes(int64_t n, int algo) {
+  if (n <= 0) return 0;
+  if (algo == EDPP_SCAN_LOOKBACK) return kHeader + LookbackState<T>::bytes(tiles_of<T>(n));
+  return kHeader + round_up(static_cast<size_t>(kMaxChunkBlocks) * sizeof(T), 256);
+}
+
+// Blocks of the RTS / SSA schemes: a few waves of resident blocks, each
+// owning a contiguous run of whole tiles.
+template <typename T> void chunk_grid(int64_t n, int64_t &blocks, int64_t &tpb) {
+  const int64_t tiles = tiles_of<T>(n);
+  int64_t g = static_cast<int64_t>(device_sm_count()) * 4;
+  g = std::min<int64_t>(g, kMaxChunkBlocks);
+  g = std::min<int64_t>(g, tiles);
+  tpb = (tiles + g - 1) / g;
+  blocks = (tiles + tpb - 1) / tpb;
+}
+
+template <typename T, bool kInclusive>
+int scan_impl(const T *in, T *out, int64_t n, int algo, void *ws, size_t ws_bytes, void *stream,
+              int64_t ticket_base = 0, uint64_t timeout_ns = kDefaultWaitNs) {
+  if (n < 0) return EDPP_EINVAL;
+  if (algo != EDPP_SCAN_LOOKBACK && algo != EDPP_SCAN_RTS && algo != EDPP_SCAN_SSA)
+    return EDPP_EINVAL;
+  if (n == 0) return EDPP_OK;
+  if (!in || !out) return EDPP_EINVAL;
+  const size_t need = workspace_bytes<T>(n, algo);
+  if (!ws || ws_bytes < need) return EDPP_ENOMEM;
+  cudaStream_t st = as_stream(stream);
+  unsigned *fault = fault_word();
+  if (!fault) return EDPP_ECUDA;
+  const bool tma = aligned16(in);
+  const bool vec_out = aligned16(out);
+  char *w = static_cast<char *>(ws);
+
+  if (algo == EDPP_SCAN_LOOKBACK) {
+    const int64_t tiles = tiles_of<T>(n);
+    if (cudaMemsetAsync(ws, 0, need, st) != cudaSuccess) return EDPP_ECUDA;
+    LookbackState<T> state;
+    state.bind(w + kHeader, tiles);
+    scan_lookback_kernel<T, kInclusive><<<static_cast<unsigned>(tiles), kThreads, 0, st>>>(
+        in, out, n, tiles, reinterpret_cast<unsigned long long *>(w), state, ticket_base, tma,
+        vec_out, timeout_ns, fault);
+    return launch_status();
+  }
+
+  int64_t blocks, tpb;
+  chunk_grid<T>(n, blocks, tpb);
+  T *partials = reinterpret_cast<T *>(w + kHeader);
+  const int64_t per = tpb * TS<T>::kTile;
+  if (algo == EDPP_SCAN_RTS) {
+    reduce_blocks_kernel<T><<<static_cast<unsigned>(blocks), kThreads, 0, st>>>(in, n, per,
+                                                                                partials, tma);
+    scan_partials_kernel<T><<<1, 1024, 0, st>>>(partials, static_cast<int>(blocks));
+    scan_blocks_kernel<T, kInclusive, true><<<static_cast<unsigned>(blocks), kThreads, 0, st>>>(
+        in, out, n, tpb, partials, nullptr, tma, vec_out, timeout_ns, fault);
+  } else {  // SSA
+    scan_blocks_kernel<T, kInclusive, false><<<static_cast<unsigned>(blocks), kThreads, 0, st>>>(
+        in, out, n, tpb, nullptr, partials, tma, vec_out, timeout_ns, fault);
+    scan_partials_kernel<T><<<1, 1024, 0, st>>>(partials, static_cast<int>(blocks));
+    add_offsets_kernel<T><<<static_cast<unsigned>(blocks), kThreads, 0, st>>>(out, n, per,
+                                                                             partials, vec_out);
+  }
+  return launch_status();
+}
+
+}  // namespace
+}  // namespace edpp
+
+extern "C" {
+
+size_t edpp_scan_workspace_size(int64_t length, int dtype, int algo) {
+  switch (dtype) {
+    case EDPP_I32: return edpp::workspace_bytes<int32_t>(length, algo);
+    case EDPP_I64: return edpp::workspace_bytes<int64_t>(length, algo);
+    case EDPP_F32: return edpp::workspace_bytes<float>(length, algo);
+    default: return 0;
+  }
+}
+
+int edpp_scan_exclusive_i32(const int32_t *in, int32_t *out, int64_t length, int algo, void *ws,
+                            size_t ws_bytes, void *stream) {
+  return edpp::scan_impl<int32_t, false>(in, out, length, algo, ws, ws_bytes, stream);
+}
+int edpp_scan_inclusive_i32(const int32_t *in, int32_t *out, int64_t length, int algo, void *ws,
+                            size_t ws_bytes, void *stream) {
+  return edpp::scan_impl<int32_t, true>(in, out, length, algo, ws, ws_bytes, stream);
+}
+int edpp_scan_exclusive_i64(const int64_t *in, int64_t *out, int64_t length, int algo, void *ws,
+                            size_t ws_bytes, void *stream) {
+  return edpp::scan_impl<int64_t, false>(in, out, length, algo, ws, ws_bytes, stream);
+}
+int edpp_scan_inclusive_i64(const int64_t *in, int64_t *out, int64_t length, int algo, void *ws,
+                            size_t ws_bytes, void *stream) {
+  return edpp::scan_impl<int64_t, true>(in, out, length, algo, ws, ws_bytes, stream);
+}
+int edpp_scan_exclusive_f32(const float *in, float *out, int64_t length, int algo, void *ws,
+                            size_t ws_bytes, void *stream) {
+  return edpp::scan_impl<float, false>(in, out, length, algo, ws, ws_bytes, stream);
+}
+int edpp_scan_inclusive_f32(const float *in, float *out, int64_t length, int algo, void *ws,
+                            size_t ws_bytes, void *stream) {
+  return edpp::scan_impl<float, true>(in, out, length, algo, ws, ws_bytes, stream);
+}
+
+int edpp_selftest_lookback_timeout(const int32_t *in, int32_t *out, int64_t length,
+                                   uint64_t timeout_ns, void *ws, size_t ws_bytes, void *stream) {
+  if (length <= 0 || timeout_ns == 0) return EDPP_EINVAL;
+  // Tickets start at tile 1: tile 0 is never scanned, so tile 1 (and every
+  // later tile) waits for a prefix nobody publishes until the limit runs out.
+  return edpp::scan_impl<int32_t, false>(in, out, length, EDPP_SCAN_LOOKBACK, ws, ws_bytes, stream,
+                                         /*ticket_base=*/1, timeout_ns);
+}
+
+}  // extern "C"

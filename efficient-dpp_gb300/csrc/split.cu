@@ -1,0 +1,410 @@
+// split.cu — stable multi-split of int32 keys (KO), key/value arrays
+// (KVS_SOA) or {key,value} pairs (KVS_AOS) by bucket = key & (B-1).
+//
+// Same three stages as the reference's split (histogram -> scan of the
+// bucket-major histogram -> shuffle; opencl/primitives/splitImpl.cpp:66-140,
+// cuda/test_split.cu:149-186), re-planned for GB300:
+//
+//  1. hist:    one block per tile of kTile elements counts its buckets with
+//              warp-aggregated shared-memory atomics (__match_any_sync groups
+//              the lanes of a bucket; one leader adds the group size) and
+//              writes column t of the bucket-major matrix his[b*T + t], the
+//              layout of WI/WG_histogram (split_kernel.cl:370,451) and of
+//              warp_histogram (cuda/test_split.cu:48).
+//  2. scan:    exclusive look-back scan of his[] in place (scan.cu), as the
+//              reference runs scan_chained(d_his, d_his, ...) in place
+//              (splitImpl.cpp:97).  his[b*T + t] is then the first output
+//              index of bucket b's elements from tile t.
+//  3. scatter: one block per tile stages the tile in shared memory by TMA
+//              bulk copy; every warp ranks its contiguous 1/WARPS of the tile
+//              in input order (peer group from __match_any_sync, rank = popc
+//              of lower peers + the warp's running count of the bucket, kept
+//              as 16-bit counters in shared memory); ranks of all warps are
+//              combined per bucket, the tile is re-laid out in shared memory
+//              in bucket order, and written out as one contiguous run per
+//              bucket (coalesced), at his[b*T + t] + rank.
+//
+// Ranks follow input order inside a warp segment, warp segments follow
+// input order inside a tile, tiles follow input order in the scan: the split
+// is stable, bit-identical to single_split (split_kernel.cl:676-736),
+// WG_split with FIXED_REORDER and the CUDA pre_scan/post_scan split.  There
+// are no inter-block waits.
+#include <mutex>
+
+#include "common.cuh"
+
+namespace edpp {
+namespace {
+
+constexpr int kTile = 8192;
+constexpr int kMaxBuckets = 4096;
+constexpr int kHistThreads = 512;
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// Key of element i.
+template <int LAYOUT> __device__ __forceinline__ int32_t key_at(const int32_t *k, int64_t i) {
+  return LAYOUT == EDPP_KVS_AOS ? k[2 * i] : k[i];
+}
+
+// ---- stage 1: per-tile bucket counts ----------------------------------------
+template <int LAYOUT>
+__global__ void __launch_bounds__(kHistThreads)
+    split_hist_kernel(const int32_t *__restrict__ keys, int64_t n, int buckets, int64_t tiles,
+                      int32_t *__restrict__ his, bool vec) {
+  __shared__ uint32_t cnt[kMaxBuckets];
+  const unsigned mask = static_cast<unsigned>(buckets - 1);
+  for (int b = threadIdx.x; b < buckets; b += kHistThreads) cnt[b] = 0;
+  __syncthreads();
+  const int64_t t = blockIdx.x;
+  const int64_t base = t * kTile;
+  const int count = static_cast<int>(min64(kTile, n - base));
+  const unsigned lt = lanemask_lt();
+
+  auto add = [&](bool valid, int32_t key) {
+    const int b = valid ? static_cast<int>(static_cast<unsigned>(key) & mask) : -1;
+    const unsigned peers = __match_any_sync(0xffffffffu, b);
+    if (valid && (peers & lt) == 0u) atomicAdd(&cnt[b], static_cast<uint32_t>(__popc(peers)));
+  };
+
+  if (LAYOUT != EDPP_KVS_AOS && vec && count == kTile) {
+    // 16-byte vectors, warp-contiguous: 4 keys per thread per step.
+    const int4 *k4 = reinterpret_cast<const int4 *>(keys + base);
+#pragma unroll 2
+    for (int v = threadIdx.x; v < kTile / 4; v += kHistThreads) {
+      const int4 q = __ldcs(k4 + v);
+      add(true, q.x);
+      add(true, q.y);
+      add(true, q.z);
+      add(true, q.w);
+    }
+  } else if (LAYOUT == EDPP_KVS_AOS && vec && count == kTile) {
+    // 16-byte vectors of two pairs.
+    const int4 *p4 = reinterpret_cast<const int4 *>(keys + 2 * base);
+#pragma unroll 2
+    for (int v = threadIdx.x; v < kTile / 2; v += kHistThreads) {
+      const int4 q = __ldcs(p4 + v);
+      add(true, q.x);
+      add(true, q.z);
+    }
+  } else {
+    for (int i0 = 0; i0 < count; i0 += kHistThreads) {
+      const int i = i0 + threadIdx.x;
+      const bool valid = i < count;
+      add(valid, valid ? key_at<LAYOUT>(keys, base + i) : 0);
+    }
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < buckets; b += kHistThreads)
+    his[static_cast<int64_t>(b) * tiles + t] = static_cast<int32_t>(cnt[b]);
+}
+
+// ---- stage 3: stable scatter --------------------------------------------------
+template <int THREADS> struct ScatterCfg {
+  static constexpr int kWarps = THREADS / 32;
+  static constexpr int kSeg = kTile / kWarps;  // elements per warp
+  static constexpr int kIters = kSeg / 32;     // per lane
+};
+
+// Dynamic shared memory of the scatter kernel.
+template <int THREADS, int LAYOUT> size_t scatter_smem_bytes(int buckets) {
+  const size_t stage = (LAYOUT == EDPP_KO) ? kTile * 4 : kTile * 8;
+  return stage + round_up(static_cast<size_t>(ScatterCfg<THREADS>::kWarps) * buckets * 2, 16) +
+         2 * static_cast<size_t>(buckets) * 4;
+}
+
+template <int THREADS, int LAYOUT>
+__global__ void __launch_bounds__(THREADS)
+    split_scatter_kernel(const int32_t *__restrict__ keys_in, int32_t *__restrict__ keys_out,
+                         const int32_t *__restrict__ vals_in, int32_t *__restrict__ vals_out,
+                         int64_t n, int buckets, int64_t tiles, const int32_t *__restrict__ his,
+                         bool tma, uint64_t timeout_ns, unsigned *fault) {
+  using C = ScatterCfg<THREADS>;
+  constexpr bool kKV = LAYOUT != EDPP_KO;
+  extern __shared__ __align__(128) unsigned char smem[];
+  // Layout: stage (keys[kTile] + vals[kTile], or pairs[kTile]) | cnt16 | toff | gofs
+  int32_t *s_keys = reinterpret_cast<int32_t *>(smem);
+  int32_t *s_vals = s_keys + kTile;  // SOA only
+  int2 *s_pairs = reinterpret_cast<int2 *>(smem);  // AOS only
+  const size_t stage = kKV ? kTile * 8 : kTile * 4;
+  uint16_t *cnt16 = reinterpret_cast<uint16_t *>(smem + stage);
+  int32_t *toff = reinterpret_cast<int32_t *>(
+      smem + stage + round_up(static_cast<size_t>(C::kWarps) * buckets * 2, 16));
+  int32_t *gofs = toff + buckets;
+  __shared__ alignas(8) uint64_t bar;
+
+  const int64_t t = blockIdx.x;
+  const int64_t base = t * kTile;
+  const int count = static_cast<int>(min64(kTile, n - base));
+  const unsigned mask = static_cast<unsigned>(buckets - 1);
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+
+  // -- load the tile (bulk copies for the 16-byte-aligned prefix) --
+  if (tid == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  uint32_t bulk_elems = 0;
+  if (tma) bulk_elems = (LAYOUT == EDPP_KVS_AOS) ? (count & ~1) : (count & ~3);
+  if (tid == 0 && bulk_elems) {
+    if (LAYOUT == EDPP_KVS_AOS) {
+      mbar_arrive_expect_tx(&bar, bulk_elems * 8);
+      tma_load_1d(s_pairs, keys_in + 2 * base, bulk_elems * 8, &bar);
+    } else if (LAYOUT == EDPP_KVS_SOA) {
+      mbar_arrive_expect_tx(&bar, bulk_elems * 8);
+      tma_load_1d(s_keys, keys_in + base, bulk_elems * 4, &bar);
+      tma_load_1d(s_vals, vals_in + base, bulk_elems * 4, &bar);
+    } else {
+      mbar_arrive_expect_tx(&bar, bulk_elems * 4);
+      tma_load_1d(s_keys, keys_in + base, bulk_elems * 4, &bar);
+    }
+  }
+  for (int i = static_cast<int>(bulk_elems) + tid; i < count; i += THREADS) {
+    if (LAYOUT == EDPP_KVS_AOS) {
+      s_pairs[i] = make_int2(keys_in[2 * (base + i)], keys_in[2 * (base + i) + 1]);
+    } else {
+      s_keys[i] = keys_in[base + i];
+      if (LAYOUT == EDPP_KVS_SOA) s_vals[i] = vals_in[base + i];
+    }
+  }
+  for (int i = tid; i < C::kWarps * buckets; i += THREADS) cnt16[i] = 0;
+  if (bulk_elems) {
+    if (!mbar_wait_bounded(&bar, 0, timeout_ns, fault)) return;
+  }
+  __syncthreads();
+
+  // -- rank: warp w owns tile positions [w*kSeg, (w+1)*kSeg), in order --
+  const unsigned lt = lanemask_lt();
+  uint16_t *my_cnt = cnt16 + w * buckets;
+  int32_t kk[C::kIters];
+  int32_t vv[C::kIters];
+  uint32_t rk[(C::kIters + 1) / 2];  // two 16-bit ranks per register
+#pragma unroll
+  for (int it = 0; it < C::kIters; ++it) {
+    const int pos = w * C::kSeg + it * 32 + lane;
+    const bool valid = pos < count;
+    int32_t key = 0, val = 0;
+    if (valid) {
+      if (LAYOUT == EDPP_KVS_AOS) {
+        const int2 p = s_pairs[pos];
+        key = p.x;
+        val = p.y;
+      } else {
+        key = s_keys[pos];
+        if (LAYOUT == EDPP_KVS_SOA) val = s_vals[pos];
+      }
+    }
+    const int b = valid ? static_cast<int>(static_cast<unsigned>(key) & mask) : -1;
+    const unsigned peers = __match_any_sync(0xffffffffu, b);
+    const unsigned lower = peers & lt;
+    const uint16_t before = valid ? my_cnt[b] : 0;
+    __syncwarp();
+    if (valid && lower == 0u) my_cnt[b] = static_cast<uint16_t>(before + __popc(peers));
+    __syncwarp();
+    kk[it] = key;
+    vv[it] = val;
+    const uint32_t r = static_cast<uint32_t>(before + __popc(lower));
+    if (it & 1) rk[it >> 1] |= r << 16;
+    else rk[it >> 1] = r;
+  }
+  __syncthreads();
+
+  // -- per bucket: exclusive prefix over warps, tile count, tile offsets --
+  // Thread-consecutive buckets so the block-wide scan over buckets is a
+  // per-thread serial scan plus one warp/ block combine.
+  const int per = (buckets + THREADS - 1) / THREADS;
+  const int b_lo = min(buckets, tid * per), b_hi = min(buckets, b_lo + per);
+  int32_t my_total = 0;
+  for (int b = b_lo; b < b_hi; ++b) {
+    int32_t run = 0;
+#pragma unroll 4
+    for (int ww = 0; ww < C::kWarps; ++ww) {
+      const int32_t c = cnt16[ww * buckets + b];
+      cnt16[ww * buckets + b] = static_cast<uint16_t>(run);
+      run += c;
+    }
+    toff[b] = run;  // tile count for now
+    my_total += run;
+  }
+  // Block exclusive scan of my_total.
+  __shared__ int32_t s_wsum[32];
+  int32_t incl = my_total;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d) incl += y;
+  }
+  if (lane == 31) s_wsum[w] = incl;
+  __syncthreads();
+  if (w == 0) {
+    const int32_t x = lane < C::kWarps ? s_wsum[lane] : 0;
+    int32_t xi = x;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int32_t y = __shfl_up_sync(0xffffffffu, xi, d);
+      if (lane >= d) xi += y;
+    }
+    if (lane < C::kWarps) s_wsum[lane] = xi - x;
+  }
+  __syncthreads();
+  int32_t run = s_wsum[w] + (incl - my_total);
+  for (int b = b_lo; b < b_hi; ++b) {
+    const int32_t c = toff[b];
+    toff[b] = run;
+    // First output index of bucket b from this tile, minus its tile offset.
+    gofs[b] = his[static_cast<int64_t>(b) * tiles + t] - run;
+    run += c;
+  }
+  __syncthreads();
+
+  // -- re-lay the tile out in bucket order (stable) --
+#pragma unroll
+  for (int it = 0; it < C::kIters; ++it) {
+    const int pos = w * C::kSeg + it * 32 + lane;
+    if (pos < count) {
+      const int b = static_cast<int>(static_cast<unsigned>(kk[it]) & mask);
+      const int r = static_cast<int>((rk[it >> 1] >> ((it & 1) * 16)) & 0xffffu);
+      const int s = toff[b] + cnt16[w * buckets + b] + r;
+      if (LAYOUT == EDPP_KVS_AOS) {
+        s_pairs[s] = make_int2(kk[it], vv[it]);
+      } else {
+        s_keys[s] = kk[it];
+        if (LAYOUT == EDPP_KVS_SOA) s_vals[s] = vv[it];
+      }
+    }
+  }
+  __syncthreads();
+
+  // -- write out: consecutive threads write consecutive slots of a bucket run --
+  for (int s = tid; s < count; s += THREADS) {
+    if (LAYOUT == EDPP_KVS_AOS) {
+      const int2 p = s_pairs[s];
+      const int b = static_cast<int>(static_cast<unsigned>(p.x) & mask);
+      reinterpret_cast<int2 *>(keys_out)[gofs[b] + s] = p;
+    } else {
+      const int32_t key = s_keys[s];
+      const int b = static_cast<int>(static_cast<unsigned>(key) & mask);
+      const int64_t o = static_cast<int64_t>(gofs[b]) + s;
+      keys_out[o] = key;
+      if (LAYOUT == EDPP_KVS_SOA) vals_out[o] = s_vals[s];
+    }
+  }
+}
+
+// bucket_start[b] = his[b*T] (gatherStartPos, split_kernel.cl:320-332).
+__global__ void bucket_start_kernel(const int32_t *his, int64_t tiles, int buckets,
+                                    int32_t *start) {
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < buckets; b += gridDim.x * blockDim.x)
+    start[b] = his[static_cast<int64_t>(b) * tiles];
+}
+
+size_t his_bytes(int64_t tiles, int buckets) {
+  return round_up(static_cast<size_t>(tiles) * buckets * 4, 256);
+}
+
+template <int THREADS, int LAYOUT> int set_smem_attr() {
+  static std::once_flag once[64];
+  static int status[64];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  std::call_once(once[dev], [&] {
+    const size_t bytes = scatter_smem_bytes<THREADS, LAYOUT>(kMaxBuckets);
+    status[dev] = cuda_status(cudaFuncSetAttribute(split_scatter_kernel<THREADS, LAYOUT>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   static_cast<int>(bytes)));
+  });
+  return status[dev];
+}
+
+template <int THREADS, int LAYOUT>
+int launch_scatter(const int32_t *keys_in, int32_t *keys_out, const int32_t *vals_in,
+                   int32_t *vals_out, int64_t n, int buckets, int64_t tiles, const int32_t *his,
+                   bool tma, cudaStream_t st) {
+  const int s = set_smem_attr<THREADS, LAYOUT>();
+  if (s != EDPP_OK) return s;
+  const size_t smem = scatter_smem_bytes<THREADS, LAYOUT>(buckets);
+  split_scatter_kernel<THREADS, LAYOUT><<<static_cast<unsigned>(tiles), THREADS, smem, st>>>(
+      keys_in, keys_out, vals_in, vals_out, n, buckets, tiles, his, tma, kDefaultWaitNs,
+      fault_word());
+  return launch_status();
+}
+
+template <int LAYOUT>
+int split_layout(const int32_t *keys_in, int32_t *keys_out, int32_t *bucket_start, int64_t n,
+                 int buckets, const int32_t *vals_in, int32_t *vals_out, void *ws, size_t ws_bytes,
+                 cudaStream_t st) {
+  const int64_t tiles = (n + kTile - 1) / kTile;
+  int32_t *his = static_cast<int32_t *>(ws);
+  const int64_t hlen = tiles * buckets;
+  void *scan_ws = static_cast<char *>(ws) + his_bytes(tiles, buckets);
+  const size_t scan_ws_bytes = ws_bytes - his_bytes(tiles, buckets);
+  bool tma = aligned16(keys_in) && (LAYOUT != EDPP_KVS_SOA || aligned16(vals_in));
+  split_hist_kernel<LAYOUT><<<static_cast<unsigned>(tiles), kHistThreads, 0, st>>>(
+      keys_in, n, buckets, tiles, his, aligned16(keys_in));
+  int s = launch_status();
+  if (s != EDPP_OK) return s;
+  s = edpp_scan_exclusive_i32(his, his, hlen, EDPP_SCAN_LOOKBACK, scan_ws, scan_ws_bytes, st);
+  if (s != EDPP_OK) return s;
+  if (bucket_start) {
+    bucket_start_kernel<<<(buckets + 255) / 256, 256, 0, st>>>(his, tiles, buckets, bucket_start);
+    s = launch_status();
+    if (s != EDPP_OK) return s;
+  }
+  if (buckets <= 1024)
+    return launch_scatter<512, LAYOUT>(keys_in, keys_out, vals_in, vals_out, n, buckets, tiles, his,
+                                       tma, st);
+  return launch_scatter<256, LAYOUT>(keys_in, keys_out, vals_in, vals_out, n, buckets, tiles, his,
+                                     tma, st);
+}
+
+size_t split_ws_bytes(int64_t n, int buckets) {
+  if (n <= 0 || buckets < 1) return 0;
+  const int64_t tiles = (n + kTile - 1) / kTile;
+  return his_bytes(tiles, buckets) +
+         edpp_scan_workspace_size(tiles * buckets, EDPP_I32, EDPP_SCAN_LOOKBACK);
+}
+
+}  // namespace
+}  // namespace edpp
+
+extern "C" {
+
+size_t edpp_split_workspace_size(int64_t length, int buckets, int layout) {
+  (void)layout;
+  if (buckets < 1 || buckets > edpp::kMaxBuckets || (buckets & (buckets - 1))) return 0;
+  return edpp::split_ws_bytes(length, buckets);
+}
+
+int edpp_split_i32(const int32_t *keys_in, int32_t *keys_out, int32_t *bucket_start,
+                   int64_t length, int buckets, int layout, const int32_t *vals_in,
+                   int32_t *vals_out, void *ws, size_t ws_bytes, void *stream) {
+  if (length < 0 || length > INT32_MAX) return EDPP_EINVAL;
+  if (buckets < 1 || buckets > edpp::kMaxBuckets || (buckets & (buckets - 1))) return EDPP_EINVAL;
+  if (layout != EDPP_KO && layout != EDPP_KVS_AOS && layout != EDPP_KVS_SOA) return EDPP_EINVAL;
+  if (length == 0) return EDPP_OK;
+  if (!keys_in || !keys_out) return EDPP_EINVAL;
+  // SOA needs both value arrays (splitImpl.cpp:29-34 returns -1 otherwise).
+  if (layout == EDPP_KVS_SOA && (!vals_in || !vals_out)) return EDPP_EINVAL;
+  const size_t need = edpp::split_ws_bytes(length, buckets);
+  if (!ws || ws_bytes < need) return EDPP_ENOMEM;
+  cudaStream_t st = edpp::as_stream(stream);
+  switch (layout) {
+    case EDPP_KO:
+      return edpp::split_layout<EDPP_KO>(keys_in, keys_out, bucket_start, length, buckets, nullptr,
+                                         nullptr, ws, ws_bytes, st);
+    case EDPP_KVS_SOA:
+      return edpp::split_layout<EDPP_KVS_SOA>(keys_in, keys_out, bucket_start, length, buckets,
+                                              vals_in, vals_out, ws, ws_bytes, st);
+    default:
+      return edpp::split_layout<EDPP_KVS_AOS>(keys_in, keys_out, bucket_start, length, buckets,
+                                              nullptr, nullptr, ws, ws_bytes, st);
+  }
+}
+
+}  // extern "C"

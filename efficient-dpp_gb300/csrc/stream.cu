@@ -1,0 +1,162 @@
+// stream.cu — STREAM copy / scale / add / triad.
+//
+// Replaces the one-element-per-thread kernels of cuda/test_bandwidth.cu:14-44
+// and opencl/kernels/mem_kernel.cl:9-31 (int32, SCALAR=3) with a 128-bit
+// vectorised, grid-stride form: every thread keeps kUnroll 16-byte loads of
+// each input in flight before its stores, and the grid is a whole number of
+// waves over the SMs.  Loads and stores carry the streaming (evict-first)
+// cache hint, since every byte is touched exactly once.
+#include "common.cuh"
+
+namespace edpp {
+namespace {
+
+enum StreamOp { kCopy = 0, kScale = 1, kAdd = 2, kTriad = 3 };
+
+template <typename T> struct Vec4;
+template <> struct Vec4<float> { using type = float4; };
+template <> struct Vec4<int32_t> { using type = int4; };
+
+// Integer arithmetic wraps (two's complement), as int32 STREAM does on the
+// reference's platforms.
+__device__ __forceinline__ int32_t mul_wrap(int32_t a, int32_t s) {
+  return static_cast<int32_t>(static_cast<uint32_t>(a) * static_cast<uint32_t>(s));
+}
+__device__ __forceinline__ int32_t add_wrap(int32_t a, int32_t b) {
+  return static_cast<int32_t>(static_cast<uint32_t>(a) + static_cast<uint32_t>(b));
+}
+__device__ __forceinline__ float mul_wrap(float a, float s) { return a * s; }
+__device__ __forceinline__ float add_wrap(float a, float b) { return a + b; }
+
+template <int OP, typename T>
+__device__ __forceinline__ T apply(T a, T b, T s) {
+  if (OP == kCopy) return a;
+  if (OP == kScale) return mul_wrap(a, s);
+  if (OP == kAdd) return add_wrap(a, b);
+  return add_wrap(a, mul_wrap(b, s));  // triad: a + s*b
+}
+
+template <int OP, typename V, typename T>
+__device__ __forceinline__ V apply4(const V &a, const V &b, T s) {
+  V r;
+  r.x = apply<OP>(a.x, b.x, s);
+  r.y = apply<OP>(a.y, b.y, s);
+  r.z = apply<OP>(a.z, b.z, s);
+  r.w = apply<OP>(a.w, b.w, s);
+  return r;
+}
+
+constexpr int kThreads = 256;
+constexpr int kUnroll = 4;
+
+// Vector body: n4 16-byte vectors, grid-stride with kUnroll vectors per
+// thread per step.  Then the scalar tail [4*n4, n) by the first threads.
+template <int OP, typename T>
+__global__ void __launch_bounds__(kThreads)
+    stream_vec_kernel(const T *__restrict__ a, const T *__restrict__ b, T *__restrict__ c, T s,
+                      int64_t n) {
+  using V = typename Vec4<T>::type;
+  const V *a4 = reinterpret_cast<const V *>(a);
+  const V *b4 = reinterpret_cast<const V *>(b);
+  V *c4 = reinterpret_cast<V *>(c);
+  const int64_t n4 = n >> 2;
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * kThreads;
+  int64_t i = static_cast<int64_t>(blockIdx.x) * kThreads + threadIdx.x;
+  const bool two = (OP == kAdd || OP == kTriad);
+
+  // Full unrolled steps.
+  for (; i + (kUnroll - 1) * stride < n4; i += kUnroll * stride) {
+    V va[kUnroll], vb[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) {
+      va[u] = __ldcs(a4 + i + u * stride);
+      vb[u] = two ? __ldcs(b4 + i + u * stride) : va[u];
+    }
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) __stcs(c4 + i + u * stride, apply4<OP>(va[u], vb[u], s));
+  }
+  // Remaining vectors.
+  for (; i < n4; i += stride) {
+    V va = __ldcs(a4 + i);
+    V vb = va;
+    if (two) vb = __ldcs(b4 + i);
+    __stcs(c4 + i, apply4<OP>(va, vb, s));
+  }
+  // Scalar tail.
+  if (blockIdx.x == 0 && threadIdx.x < (n & 3)) {
+    const int64_t j = (n4 << 2) + threadIdx.x;
+    c[j] = apply<OP>(a[j], two ? b[j] : a[j], s);
+  }
+}
+
+// Unaligned fallback: scalar grid-stride.
+template <int OP, typename T>
+__global__ void __launch_bounds__(kThreads)
+    stream_scalar_kernel(const T *__restrict__ a, const T *__restrict__ b, T *__restrict__ c, T s,
+                         int64_t n) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * kThreads;
+  const bool two = (OP == kAdd || OP == kTriad);
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * kThreads + threadIdx.x; i < n; i += stride)
+    c[i] = apply<OP>(a[i], two ? b[i] : a[i], s);
+}
+
+template <int OP, typename T>
+int launch_stream(const T *a, const T *b, T *c, T s, int64_t n, void *stream) {
+  const bool two = (OP == kAdd || OP == kTriad);
+  if (n < 0 || (n > 0 && (!a || !c || (two && !b)))) return EDPP_EINVAL;
+  if (n == 0) return EDPP_OK;
+  cudaStream_t st = as_stream(stream);
+  const int sms = device_sm_count();
+  // Enough resident warps to cover HBM latency: 8 blocks of 256 per SM, but
+  // never more blocks than there is work for.
+  const int64_t per_block = static_cast<int64_t>(kThreads) * 4 * kUnroll;
+  int64_t blocks = (n + per_block - 1) / per_block;
+  const int64_t cap = static_cast<int64_t>(sms) * 8;
+  if (blocks > cap) blocks = cap;
+  if (blocks < 1) blocks = 1;
+  const bool vec = aligned16(a) && aligned16(c) && (!two || aligned16(b));
+  if (vec)
+    stream_vec_kernel<OP, T><<<static_cast<unsigned>(blocks), kThreads, 0, st>>>(a, b, c, s, n);
+  else
+    stream_scalar_kernel<OP, T><<<static_cast<unsigned>(blocks), kThreads, 0, st>>>(a, b, c, s, n);
+  return launch_status();
+}
+
+}  // namespace
+}  // namespace edpp
+
+using edpp::kAdd;
+using edpp::kCopy;
+using edpp::kScale;
+using edpp::kTriad;
+
+extern "C" {
+
+int edpp_stream_copy_f32(const float *a, float *c, int64_t n, void *stream) {
+  return edpp::launch_stream<kCopy, float>(a, nullptr, c, 0.f, n, stream);
+}
+int edpp_stream_scale_f32(const float *a, float *c, float s, int64_t n, void *stream) {
+  return edpp::launch_stream<kScale, float>(a, nullptr, c, s, n, stream);
+}
+int edpp_stream_add_f32(const float *a, const float *b, float *c, int64_t n, void *stream) {
+  return edpp::launch_stream<kAdd, float>(a, b, c, 0.f, n, stream);
+}
+int edpp_stream_triad_f32(const float *a, const float *b, float *c, float s, int64_t n,
+                          void *stream) {
+  return edpp::launch_stream<kTriad, float>(a, b, c, s, n, stream);
+}
+int edpp_stream_copy_i32(const int32_t *a, int32_t *c, int64_t n, void *stream) {
+  return edpp::launch_stream<kCopy, int32_t>(a, nullptr, c, 0, n, stream);
+}
+int edpp_stream_scale_i32(const int32_t *a, int32_t *c, int32_t s, int64_t n, void *stream) {
+  return edpp::launch_stream<kScale, int32_t>(a, nullptr, c, s, n, stream);
+}
+int edpp_stream_add_i32(const int32_t *a, const int32_t *b, int32_t *c, int64_t n, void *stream) {
+  return edpp::launch_stream<kAdd, int32_t>(a, b, c, 0, n, stream);
+}
+int edpp_stream_triad_i32(const int32_t *a, const int32_t *b, int32_t *c, int32_t s, int64_t n,
+                          void *stream) {
+  return edpp::launch_stream<kTriad, int32_t>(a, b, c, s, n, stream);
+}
+
+}  // extern "C"

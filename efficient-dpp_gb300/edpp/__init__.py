@@ -1,0 +1,315 @@
+"""edpp — Python host layer over libedpp's C ABI (include/edpp.h).
+
+The primitives run as hand-written sm_103a CUDA kernels inside libedpp.so;
+this module only binds the C ABI with ctypes, takes PyTorch CUDA tensors for
+device memory and streams, and raises on a non-zero status.  There is no CPU
+fallback: without the built library every call raises EdppError.
+
+Device calls (tensors must be on a CUDA device, contiguous):
+    gather(inp, loc, passes=1, out=None)        out[i] = inp[loc[i]]
+    scatter(inp, loc, passes=1, out=None)       out[loc[i]] = inp[i]
+    scan(x, inclusive=False, algo="lookback")   prefix sums (int32/int64/f32)
+    split(keys, buckets, values=None, layout=)  stable multi-split
+    stream(op, a, b=None, scalar=3)             STREAM copy/scale/add/triad
+Host generators (numpy, seeded splitmix64; see csrc/host/datagen.cpp):
+    gen_uniform_i32, gen_uniform_i64, gen_uniform_f32, gen_keys_uniform,
+    gen_keys_zipf, gen_permutation
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+
+import numpy as np
+
+PKG_DIR = Path(__file__).resolve().parent.parent
+LIB_PATH = PKG_DIR / "lib" / "libedpp.so"
+
+EDPP_OK, EDPP_EINVAL, EDPP_ENOMEM, EDPP_ETIMEOUT, EDPP_ECUDA = 0, 1, 2, 3, 4
+SCAN_ALGOS = {"lookback": 0, "rts": 1, "ssa": 2}
+LAYOUTS = {"ko": 0, "aos": 1, "soa": 2}
+DTYPES = {"int32": 0, "int64": 1, "float32": 2}
+STREAM_OPS = ("copy", "scale", "add", "triad")
+
+# Every exported C entry point of include/edpp.h, with its ctypes signature.
+_VP, _I, _I64, _U64, _SZ, _F = (ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_uint64,
+                               ctypes.c_size_t, ctypes.c_float)
+SIGNATURES = {
+    "edpp_status_string": (ctypes.c_char_p, [_I]),
+    "edpp_version": (_I, []),
+    "edpp_sync_status": (_I, [_VP, _I]),
+    "edpp_device_fault": (_I, [ctypes.POINTER(ctypes.c_uint), _I]),
+    "edpp_gather_i32": (_I, [_VP, _VP, _I64, _VP, _I, _VP]),
+    "edpp_scatter_i32": (_I, [_VP, _VP, _I64, _VP, _I, _VP]),
+    "edpp_scan_workspace_size": (_SZ, [_I64, _I, _I]),
+    "edpp_scan_exclusive_i32": (_I, [_VP, _VP, _I64, _I, _VP, _SZ, _VP]),
+    "edpp_scan_inclusive_i32": (_I, [_VP, _VP, _I64, _I, _VP, _SZ, _VP]),
+    "edpp_scan_exclusive_i64": (_I, [_VP, _VP, _I64, _I, _VP, _SZ, _VP]),
+    "edpp_scan_inclusive_i64": (_I, [_VP, _VP, _I64, _I, _VP, _SZ, _VP]),
+    "edpp_scan_exclusive_f32": (_I, [_VP, _VP, _I64, _I, _VP, _SZ, _VP]),
+    "edpp_scan_inclusive_f32": (_I, [_VP, _VP, _I64, _I, _VP, _SZ, _VP]),
+    "edpp_split_workspace_size": (_SZ, [_I64, _I, _I]),
+    "edpp_split_i32": (_I, [_VP, _VP, _VP, _I64, _I, _I, _VP, _VP, _VP, _SZ, _VP]),
+    "edpp_stream_copy_f32": (_I, [_VP, _VP, _I64, _VP]),
+    "edpp_stream_scale_f32": (_I, [_VP, _VP, _F, _I64, _VP]),
+    "edpp_stream_add_f32": (_I, [_VP, _VP, _VP, _I64, _VP]),
+    "edpp_stream_triad_f32": (_I, [_VP, _VP, _VP, _F, _I64, _VP]),
+    "edpp_stream_copy_i32": (_I, [_VP, _VP, _I64, _VP]),
+    "edpp_stream_scale_i32": (_I, [_VP, _VP, ctypes.c_int32, _I64, _VP]),
+    "edpp_stream_add_i32": (_I, [_VP, _VP, _VP, _I64, _VP]),
+    "edpp_stream_triad_i32": (_I, [_VP, _VP, _VP, ctypes.c_int32, _I64, _VP]),
+    "edpp_selftest_lookback_timeout": (_I, [_VP, _VP, _I64, _U64, _VP, _SZ, _VP]),
+    # host generators
+    "edpp_gen_draw": (_U64, [_U64, _U64]),
+    "edpp_gen_uniform_i32": (None, [_VP, _I64, _U64, _I64, _I64]),
+    "edpp_gen_uniform_i64": (None, [_VP, _I64, _U64, _I64, _I64]),
+    "edpp_gen_uniform_f32": (None, [_VP, _I64, _U64, _F, _F]),
+    "edpp_gen_keys_uniform": (None, [_VP, _I64, _U64]),
+    "edpp_gen_keys_zipf": (None, [_VP, _I64, _U64, _I, ctypes.c_double]),
+    "edpp_gen_permutation_i32": (None, [_VP, _I64, _U64]),
+}
+
+
+class EdppError(RuntimeError):
+    """A C-ABI call returned a non-zero status, or the library is missing."""
+
+    def __init__(self, status: int, what: str = ""):
+        self.status = status
+        name = {1: "EINVAL", 2: "ENOMEM", 3: "ETIMEOUT", 4: "ECUDA"}.get(status, str(status))
+        super().__init__(f"edpp {what}: {name}")
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """The loaded libedpp.so (built by efficient-dpp_gb300/build.py)."""
+    global _lib
+    if _lib is None:
+        path = Path(os.environ.get("EDPP_LIB", LIB_PATH))
+        if not path.exists():
+            raise EdppError(-1, f"library not built: {path} (run __graft_entry__.build())")
+        L = ctypes.CDLL(str(path))
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(status: int, what: str = "") -> None:
+    if status != EDPP_OK:
+        raise EdppError(status, what)
+
+
+# ---------------------------------------------------------------------------
+# device helpers
+def _torch():
+    import torch  # imported lazily: the generators and the ABI load need no torch
+    return torch
+
+
+def _cuda_tensor(t, dtype=None, name="tensor"):
+    torch = _torch()
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise TypeError(f"{name} must be a CUDA tensor")
+    if not t.is_contiguous():
+        raise ValueError(f"{name} must be contiguous")
+    if dtype is not None and t.dtype != dtype:
+        raise TypeError(f"{name} must be {dtype}, got {t.dtype}")
+    return t
+
+
+def _p(t) -> ctypes.c_void_p:
+    return ctypes.c_void_p(t.data_ptr() if t is not None else 0)
+
+
+def current_stream_handle() -> ctypes.c_void_p:
+    return ctypes.c_void_p(_torch().cuda.current_stream().cuda_stream)
+
+
+def workspace(nbytes: int, device=None):
+    torch = _torch()
+    return torch.empty(max(int(nbytes), 1), dtype=torch.uint8, device=device or "cuda")
+
+
+def sync_status(clear: bool = True) -> int:
+    """Wait for the current stream; EDPP_ETIMEOUT if a bounded wait expired."""
+    return lib().edpp_sync_status(current_stream_handle(), int(clear))
+
+
+# ---------------------------------------------------------------------------
+# primitives
+def gather(inp, loc, passes: int = 1, out=None):
+    torch = _torch()
+    _cuda_tensor(inp, torch.int32, "inp")
+    _cuda_tensor(loc, torch.int32, "loc")
+    n = loc.numel()
+    if inp.numel() < n:
+        raise ValueError("inp shorter than loc")
+    if out is None:
+        out = torch.zeros(n, dtype=torch.int32, device=loc.device)
+    check(lib().edpp_gather_i32(_p(inp), _p(out), n, _p(loc), int(passes),
+                                current_stream_handle()), "gather")
+    return out
+
+
+def scatter(inp, loc, passes: int = 1, out=None):
+    torch = _torch()
+    _cuda_tensor(inp, torch.int32, "inp")
+    _cuda_tensor(loc, torch.int32, "loc")
+    n = loc.numel()
+    if out is None:
+        out = torch.zeros(n, dtype=torch.int32, device=loc.device)
+    check(lib().edpp_scatter_i32(_p(inp), _p(out), n, _p(loc), int(passes),
+                                 current_stream_handle()), "scatter")
+    return out
+
+
+_SCAN_FN = {
+    ("int32", False): "edpp_scan_exclusive_i32", ("int32", True): "edpp_scan_inclusive_i32",
+    ("int64", False): "edpp_scan_exclusive_i64", ("int64", True): "edpp_scan_inclusive_i64",
+    ("float32", False): "edpp_scan_exclusive_f32", ("float32", True): "edpp_scan_inclusive_f32",
+}
+
+
+def scan_workspace_bytes(n: int, dtype: str, algo: str = "lookback") -> int:
+    return lib().edpp_scan_workspace_size(int(n), DTYPES[dtype], SCAN_ALGOS[algo])
+
+
+def scan(x, inclusive: bool = False, algo: str = "lookback", out=None, ws=None):
+    torch = _torch()
+    _cuda_tensor(x, None, "x")
+    dt = str(x.dtype).replace("torch.", "")
+    if dt not in DTYPES:
+        raise TypeError(f"scan supports int32, int64, float32, got {x.dtype}")
+    n = x.numel()
+    if out is None:
+        out = torch.empty_like(x)
+    need = scan_workspace_bytes(n, dt, algo)
+    if ws is None:
+        ws = workspace(need, x.device)
+    fn = getattr(lib(), _SCAN_FN[(dt, bool(inclusive))])
+    check(fn(_p(x), _p(out), n, SCAN_ALGOS[algo], _p(ws), ws.numel(), current_stream_handle()),
+          "scan")
+    return out
+
+
+def split_workspace_bytes(n: int, buckets: int, layout: str = "soa") -> int:
+    return lib().edpp_split_workspace_size(int(n), int(buckets), LAYOUTS[layout])
+
+
+def split(keys, buckets: int, values=None, layout: str | None = None, bucket_start: bool = False,
+          keys_out=None, values_out=None, ws=None):
+    """Stable multi-split by key & (buckets-1).
+
+    layout "ko": keys only; "soa": keys and values tensors; "aos": keys is an
+    (n, 2) int32 tensor of {key, value} pairs.  Returns (keys_out,
+    values_out or None, bucket_start or None)."""
+    torch = _torch()
+    if layout is None:
+        layout = "ko" if values is None else "soa"
+    _cuda_tensor(keys, torch.int32, "keys")
+    if layout == "aos":
+        if keys.dim() != 2 or keys.shape[1] != 2:
+            raise ValueError("aos keys must have shape (n, 2)")
+        n = keys.shape[0]
+    else:
+        n = keys.numel()
+    if layout == "soa":
+        _cuda_tensor(values, torch.int32, "values")
+    if keys_out is None:
+        keys_out = torch.empty_like(keys)
+    if layout == "soa" and values_out is None:
+        values_out = torch.empty_like(values)
+    start = torch.empty(buckets, dtype=torch.int32, device=keys.device) if bucket_start else None
+    need = split_workspace_bytes(n, buckets, layout)
+    if ws is None:
+        ws = workspace(need, keys.device)
+    check(lib().edpp_split_i32(_p(keys), _p(keys_out), _p(start), n, int(buckets),
+                               LAYOUTS[layout], _p(values if layout == "soa" else None),
+                               _p(values_out if layout == "soa" else None), _p(ws), ws.numel(),
+                               current_stream_handle()), "split")
+    return keys_out, (values_out if layout == "soa" else None), start
+
+
+def stream(op: str, a, b=None, scalar=3, out=None):
+    torch = _torch()
+    if op not in STREAM_OPS:
+        raise ValueError(op)
+    _cuda_tensor(a, None, "a")
+    suffix = {torch.float32: "f32", torch.int32: "i32"}.get(a.dtype)
+    if suffix is None:
+        raise TypeError("stream supports float32 and int32")
+    if out is None:
+        out = torch.empty_like(a)
+    n = a.numel()
+    f = getattr(lib(), f"edpp_stream_{op}_{suffix}")
+    s = float(scalar) if suffix == "f32" else int(scalar)
+    st = current_stream_handle()
+    if op == "copy":
+        r = f(_p(a), _p(out), n, st)
+    elif op == "scale":
+        r = f(_p(a), _p(out), s, n, st)
+    elif op == "add":
+        r = f(_p(a), _p(b), _p(out), n, st)
+    else:
+        r = f(_p(a), _p(b), _p(out), s, n, st)
+    check(r, f"stream_{op}")
+    return out
+
+
+def selftest_lookback_timeout(n: int, timeout_ns: int, device="cuda") -> int:
+    """Run the look-back scan with tile 0 never published; returns the
+    status edpp_sync_status reports afterwards (EDPP_ETIMEOUT expected)."""
+    torch = _torch()
+    x = torch.ones(n, dtype=torch.int32, device=device)
+    y = torch.zeros_like(x)
+    ws = workspace(scan_workspace_bytes(n, "int32"), device)
+    check(lib().edpp_selftest_lookback_timeout(_p(x), _p(y), n, int(timeout_ns), _p(ws), ws.numel(),
+                                               current_stream_handle()), "selftest")
+    return sync_status(clear=True)
+
+
+# ---------------------------------------------------------------------------
+# seeded host generators (numpy)
+def _np_ptr(a: np.ndarray) -> ctypes.c_void_p:
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def gen_uniform_i32(n: int, seed: int, lo: int, hi: int) -> np.ndarray:
+    a = np.empty(n, dtype=np.int32)
+    lib().edpp_gen_uniform_i32(_np_ptr(a), n, seed, lo, hi)
+    return a
+
+
+def gen_uniform_i64(n: int, seed: int, lo: int, hi: int) -> np.ndarray:
+    a = np.empty(n, dtype=np.int64)
+    lib().edpp_gen_uniform_i64(_np_ptr(a), n, seed, lo, hi)
+    return a
+
+
+def gen_uniform_f32(n: int, seed: int, lo: float, hi: float) -> np.ndarray:
+    a = np.empty(n, dtype=np.float32)
+    lib().edpp_gen_uniform_f32(_np_ptr(a), n, seed, lo, hi)
+    return a
+
+
+def gen_keys_uniform(n: int, seed: int) -> np.ndarray:
+    a = np.empty(n, dtype=np.int32)
+    lib().edpp_gen_keys_uniform(_np_ptr(a), n, seed)
+    return a
+
+
+def gen_keys_zipf(n: int, seed: int, buckets: int, s: float = 1.0) -> np.ndarray:
+    a = np.empty(n, dtype=np.int32)
+    lib().edpp_gen_keys_zipf(_np_ptr(a), n, seed, buckets, s)
+    return a
+
+
+def gen_permutation(n: int, seed: int) -> np.ndarray:
+    a = np.empty(n, dtype=np.int32)
+    lib().edpp_gen_permutation_i32(_np_ptr(a), n, seed)
+    return a

@@ -1,0 +1,209 @@
+/*
+ * edpp.h — C ABI of the GB300 (sm_103a) data-parallel primitives.
+ *
+ * Every entry point is a drop-in for one primitive of Efficient-DPP's
+ * primitive API (opencl/primitives.h:12-49) or of its CUDA/OpenMP test
+ * programs, with the reference's argument order kept: input, output, length,
+ * index array, pass count, bucket count.  Differences from the reference:
+ *
+ *   - buffers are caller-owned CUDA device pointers (the reference takes
+ *     cl_mem handles); AOS key/value tuples are int32 pairs {key, value}
+ *     (the reference's cl_int2 tuple_t, opencl/types.h:47);
+ *   - calls are stream-ordered and asynchronous: they enqueue work on
+ *     `stream` (a cudaStream_t passed as void*, NULL = legacy default stream)
+ *     and return at once.  The reference calls clFinish after every launch
+ *     and returns elapsed milliseconds; edpp_primitives.hpp restores that
+ *     synchronous, time-returning form on top of this ABI;
+ *   - errors are returned as an edpp_status code, never by exit()
+ *     (the reference exits in checkErr, opencl/util/utility.cpp:85-90);
+ *   - temporaries the reference allocates per call (d_inter, d_reduction,
+ *     d_his: opencl/primitives/scanImpl.cpp:39,98, splitImpl.cpp:76,224) are
+ *     a caller-provided workspace sized by the *_workspace_size queries, so
+ *     nothing on the call path allocates;
+ *   - device-side waits (look-back, work queues) are bounded.  A wait that
+ *     runs out records EDPP_FAULT_TIMEOUT in a device fault word, the kernel
+ *     returns, and edpp_sync_status() reports EDPP_ETIMEOUT.
+ *
+ * Thread safety: calls on distinct streams with distinct workspaces may be
+ * issued from several host threads at once.  Two calls that share a
+ * workspace must be ordered on one stream.
+ */
+#ifndef EDPP_H_
+#define EDPP_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------- */
+typedef enum {
+    EDPP_OK = 0,
+    EDPP_EINVAL = 1,   /* bad argument (reference: return -1 / 1)             */
+    EDPP_ENOMEM = 2,   /* workspace too small or allocation failed            */
+    EDPP_ETIMEOUT = 3, /* a bounded device-side wait expired                  */
+    EDPP_ECUDA = 4     /* CUDA runtime error (launch, copy, sticky error)     */
+} edpp_status;
+
+/* Bits of the device fault word (edpp_device_fault). */
+#define EDPP_FAULT_TIMEOUT 0x1u   /* look-back / dependency wait ran out    */
+#define EDPP_FAULT_TMA     0x2u   /* a TMA transaction wait ran out         */
+
+/* ---- enums mirroring the reference's types (opencl/types.h:8-47) -------- */
+
+/* Global scan scheme.  LOOKBACK replaces the reference's chained
+ * (adjacent-synchronisation) scan, RTS its reduce-scan-scan (RSS) scan and
+ * SSA the scan-scan-add scheme of its OpenMP scan (openmp/test_scan_CPU.cpp). */
+typedef enum {
+    EDPP_SCAN_LOOKBACK = 0,
+    EDPP_SCAN_RTS = 1,
+    EDPP_SCAN_SSA = 2
+} edpp_scan_algo;
+
+/* Element types a scan accepts. */
+typedef enum {
+    EDPP_I32 = 0,
+    EDPP_I64 = 1,
+    EDPP_F32 = 2
+} edpp_dtype;
+
+/* Split data layout, same order as the reference's DataStruc
+ * {KO, KVS_AOS, KVS_SOA} (opencl/types.h:29-31). */
+typedef enum {
+    EDPP_KO = 0,       /* keys only                                        */
+    EDPP_KVS_AOS = 1,  /* int32 {key,value} pairs in one array             */
+    EDPP_KVS_SOA = 2   /* keys and values in two arrays                    */
+} edpp_layout;
+
+/* ---- library ------------------------------------------------------------ */
+
+/* Human-readable name of a status code. */
+const char *edpp_status_string(int status);
+
+/* Library version, as major*10000 + minor*100 + patch. */
+int edpp_version(void);
+
+/* Wait for `stream`, then report the first error: a CUDA error, or
+ * EDPP_ETIMEOUT if a kernel recorded a fault since the last clear.
+ * clear != 0 resets the fault word afterwards. */
+int edpp_sync_status(void *stream, int clear);
+
+/* Read (and optionally clear) the device fault word of the current device.
+ * Synchronises the device. */
+int edpp_device_fault(unsigned int *fault_bits, int clear);
+
+/* ---- multi-pass gather / scatter --------------------------------------- */
+
+/* out[i] = in[loc[i]] for i in [0,length).  Replaces
+ *   double gather(cl_mem d_in, cl_mem d_out, int length, cl_mem d_loc,
+ *                 int localSize, int gridSize, int pass)
+ * (opencl/primitives.h:12-14, opencl/primitives/gatherImpl.cpp:7-55,
+ *  opencl/kernels/gather_kernel.cl:6-21) and cuda/test_gather.cu:12-18.
+ * `pass` windows the source index: pass k serves loc[i] in
+ * [k*ceil(length/pass), (k+1)*ceil(length/pass)) and every pass reads all of
+ * loc, as in gatherImpl.cpp:38-53.  Entries with loc[i] outside [0,length)
+ * are skipped (out[i] keeps its value).  pass >= 1. */
+int edpp_gather_i32(const int32_t *in, int32_t *out, int64_t length,
+                    const int32_t *loc, int pass, void *stream);
+
+/* out[loc[i]] = in[i], windowed on the destination index.  Replaces
+ *   double scatter(cl_mem d_in, cl_mem d_out, int length, cl_mem d_loc,
+ *                  int localSize, int gridSize, int pass)
+ * (opencl/primitives.h:17-19, opencl/primitives/scatterImpl.cpp:9-54,
+ *  opencl/kernels/scatter_kernel.cl:6-22) and cuda/test_scatter.cu:12-18. */
+int edpp_scatter_i32(const int32_t *in, int32_t *out, int64_t length,
+                     const int32_t *loc, int pass, void *stream);
+
+/* ---- global scan -------------------------------------------------------- */
+
+/* Bytes of workspace a scan of `length` elements of `dtype` with `algo`
+ * needs (0 is a valid answer only for length 0). */
+size_t edpp_scan_workspace_size(int64_t length, int dtype, int algo);
+
+/* Exclusive / inclusive prefix sums.  Integer sums wrap (two's complement),
+ * as the reference's int scans do on its platforms; f32 sums in f32.
+ * in == out (in-place) is allowed, as split uses it at
+ * opencl/primitives/splitImpl.cpp:97.  Replaces
+ *   double scan_chained(cl_mem d_in, cl_mem d_out, int length, int localSize,
+ *                       int gridSize, int R, int L)   (LOOKBACK)
+ *   double scan_RSS(cl_mem d_in, cl_mem d_out, unsigned length,
+ *                   int local_size, int grid_size)     (RTS)
+ * (opencl/primitives.h:22-29, opencl/primitives/scanImpl.cpp:15-160),
+ * scan_SSA_omp / scan_RTS_omp (openmp/test_scan_CPU.cpp:85-163) and the CUB
+ * ExclusiveSum call of cuda/test_scan.cu:45-47. */
+int edpp_scan_exclusive_i32(const int32_t *in, int32_t *out, int64_t length,
+                            int algo, void *ws, size_t ws_bytes, void *stream);
+int edpp_scan_inclusive_i32(const int32_t *in, int32_t *out, int64_t length,
+                            int algo, void *ws, size_t ws_bytes, void *stream);
+int edpp_scan_exclusive_i64(const int64_t *in, int64_t *out, int64_t length,
+                            int algo, void *ws, size_t ws_bytes, void *stream);
+int edpp_scan_inclusive_i64(const int64_t *in, int64_t *out, int64_t length,
+                            int algo, void *ws, size_t ws_bytes, void *stream);
+int edpp_scan_exclusive_f32(const float *in, float *out, int64_t length,
+                            int algo, void *ws, size_t ws_bytes, void *stream);
+int edpp_scan_inclusive_f32(const float *in, float *out, int64_t length,
+                            int algo, void *ws, size_t ws_bytes, void *stream);
+
+/* ---- stable multi-split ------------------------------------------------- */
+
+/* Bytes of workspace a split needs. */
+size_t edpp_split_workspace_size(int64_t length, int buckets, int layout);
+
+/* Stable multi-split by bucket = key & (buckets-1): the output holds the
+ * input's elements grouped by bucket in ascending bucket order, in input
+ * order within a bucket.  buckets is a power of two in [1, 4096].
+ * bucket_start (optional, int32[buckets]) receives the first output index of
+ * every bucket, as gatherStartPos does (opencl/kernels/split_kernel.cl:320-332).
+ * KO: keys_in/keys_out hold keys, vals_* are ignored.  KVS_SOA: keys and
+ * values in separate arrays.  KVS_AOS: keys_in/keys_out point at
+ * int32 {key,value} pairs (length pairs), vals_* are ignored.
+ * Replaces WI_split / WG_split / single_split (opencl/primitives.h:32-49,
+ * opencl/primitives/splitImpl.cpp:21-498) and the warp-ballot split of
+ * cuda/test_split.cu:18-88.  The stable order is the one the reference's
+ * single_split, WG_split(FIXED_REORDER) and the CUDA split produce. */
+int edpp_split_i32(const int32_t *keys_in, int32_t *keys_out,
+                   int32_t *bucket_start, int64_t length, int buckets,
+                   int layout, const int32_t *vals_in, int32_t *vals_out,
+                   void *ws, size_t ws_bytes, void *stream);
+
+/* ---- STREAM ------------------------------------------------------------- */
+
+/* copy c=a, scale c=s*a, add c=a+b, triad c=a+s*b.  Replace the kernels of
+ * cuda/test_bandwidth.cu:14-44 and opencl/kernels/mem_kernel.cl:9-31
+ * (int32, SCALAR=3) and copy_omp/scale_omp of
+ * openmp/test_bandwidth_CPU.cpp:39-56.  Integer arithmetic wraps. */
+int edpp_stream_copy_f32(const float *a, float *c, int64_t n, void *stream);
+int edpp_stream_scale_f32(const float *a, float *c, float s, int64_t n,
+                          void *stream);
+int edpp_stream_add_f32(const float *a, const float *b, float *c, int64_t n,
+                        void *stream);
+int edpp_stream_triad_f32(const float *a, const float *b, float *c, float s,
+                          int64_t n, void *stream);
+int edpp_stream_copy_i32(const int32_t *a, int32_t *c, int64_t n,
+                         void *stream);
+int edpp_stream_scale_i32(const int32_t *a, int32_t *c, int32_t s, int64_t n,
+                          void *stream);
+int edpp_stream_add_i32(const int32_t *a, const int32_t *b, int32_t *c,
+                        int64_t n, void *stream);
+int edpp_stream_triad_i32(const int32_t *a, const int32_t *b, int32_t *c,
+                          int32_t s, int64_t n, void *stream);
+
+/* ---- bounded-wait self-test --------------------------------------------- */
+
+/* Runs a look-back scan over `length` int32 elements whose first tile is
+ * never published, with every wait limited to `timeout_ns`, so that each
+ * waiting tile gives up, records EDPP_FAULT_TIMEOUT and returns.  Exists to
+ * test failure detection without faulting the GPU; the reference's chained
+ * scan spins without a limit (opencl/kernels/scan_global_chain_kernel.cl:21).
+ * Returns the launch status; read the outcome with edpp_sync_status. */
+int edpp_selftest_lookback_timeout(const int32_t *in, int32_t *out,
+                                   int64_t length, uint64_t timeout_ns,
+                                   void *ws, size_t ws_bytes, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EDPP_H_ */
