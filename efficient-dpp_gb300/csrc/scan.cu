@@ -25,6 +25,7 @@
 // (cp.async.bulk) when the input is 16-byte aligned; see scan_tile.cuh for
 // the tile layout.
 #include <algorithm>
+#include <mutex>
 
 #include "scan_tile.cuh"
 
@@ -387,6 +388,86 @@ int edpp_selftest_lookback_timeout(const int32_t *in, int32_t *out, int64_t leng
   // later tile) waits for a prefix nobody publishes until the limit runs out.
   return edpp::scan_impl<int32_t, false>(in, out, length, EDPP_SCAN_LOOKBACK, ws, ws_bytes, stream,
                                          /*ticket_base=*/1, timeout_ns);
+}
+
+}  // extern "C"
+
+// ---- allocation-free exclusive scan -------------------------------------------
+// For callers that cannot allocate device memory: code running where
+// cudaMalloc is off limits (inside a host callback or a driver-managed region
+// that forbids new allocations, real-time loops that must not hit the
+// allocator or its implicit synchronisation, or plugins whose host application
+// owns every device allocation).  The look-back state lives in this file-scope
+// device array instead of a caller workspace.  Each GPU that loads the library
+// holds the array until the process exits.
+namespace edpp {
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = size_t(1) << 20;  // 1 MiB per device
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+// Largest length the scratch array can serve: the header plus 8 bytes of
+// look-back state per tile of TS<int32_t>::kTile elements.
+constexpr int64_t kNoAllocMaxLength =
+    static_cast<int64_t>((kNoAllocScratchBytes - kHeader) / 8) * TS<int32_t>::kTile;
+
+constexpr int kMaxDev = 64;
+std::once_flag g_noalloc_once[kMaxDev];
+void *g_noalloc_ptr[kMaxDev];
+cudaError_t g_noalloc_err[kMaxDev];
+
+// Device address of the scratch array on the current device.  In host code
+// the symbol is only a stand-in, never a usable device address, so it is
+// resolved with cudaGetSymbolAddress once per device, with that device
+// current.
+void *noalloc_scratch(cudaError_t &err) {
+  int dev = 0;
+  err = cudaGetDevice(&dev);
+  if (err != cudaSuccess) return nullptr;
+  if (dev < 0 || dev >= kMaxDev) {
+    err = cudaErrorInvalidDevice;
+    return nullptr;
+  }
+  std::call_once(g_noalloc_once[dev], [dev] {
+    void *p = nullptr;
+    g_noalloc_err[dev] = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    g_noalloc_ptr[dev] = g_noalloc_err[dev] == cudaSuccess ? p : nullptr;
+  });
+  err = g_noalloc_err[dev];
+  return g_noalloc_ptr[dev];
+}
+
+}  // namespace
+}  // namespace edpp
+
+extern "C" {
+
+int64_t edpp_scan_exclusive_i32_noalloc_max_length(void) { return edpp::kNoAllocMaxLength; }
+
+int edpp_scan_exclusive_i32_noalloc(const int32_t *in, int32_t *out, int64_t length,
+                                    void *stream) {
+  using namespace edpp;
+  if (length < 0) return EDPP_EINVAL;
+  if (length > kNoAllocMaxLength) return EDPP_EINVAL;  // beyond the static scratch
+  if (length == 0) return EDPP_OK;
+  if (!in || !out) return EDPP_EINVAL;
+  cudaError_t err;
+  char *w = static_cast<char *>(noalloc_scratch(err));
+  if (!w) return EDPP_ECUDA;
+  unsigned *fault = fault_word();
+  if (!fault) return EDPP_ECUDA;
+  cudaStream_t st = as_stream(stream);
+  const int64_t tiles = tiles_of<int32_t>(length);
+  // The array keeps the previous call's contents: clear the ticket, the
+  // abort flag and this call's look-back state before the launch.
+  const size_t used = kHeader + LookbackState<int32_t>::bytes(tiles);
+  if (cudaMemsetAsync(w, 0, used, st) != cudaSuccess) return EDPP_ECUDA;
+  LookbackState<int32_t> state;
+  state.bind(w + kHeader, tiles);
+  scan_lookback_kernel<int32_t, false><<<static_cast<unsigned>(tiles), kThreads, 0, st>>>(
+      in, out, length, tiles, reinterpret_cast<unsigned long long *>(w), state, 0,
+      aligned16(in), aligned16(out), kDefaultWaitNs, fault);
+  return launch_status();
 }
 
 }  // extern "C"

@@ -60,6 +60,8 @@ SIGNATURES = {
     "edpp_stream_add_i32": (_I, [_VP, _VP, _VP, _I64, _VP]),
     "edpp_stream_triad_i32": (_I, [_VP, _VP, _VP, ctypes.c_int32, _I64, _VP]),
     "edpp_selftest_lookback_timeout": (_I, [_VP, _VP, _I64, _U64, _VP, _SZ, _VP]),
+    "edpp_scan_exclusive_i32_noalloc": (_I, [_VP, _VP, _I64, _VP]),
+    "edpp_scan_exclusive_i32_noalloc_max_length": (_I64, []),
     # host generators
     "edpp_gen_draw": (_U64, [_U64, _U64]),
     "edpp_gen_uniform_i32": (None, [_VP, _I64, _U64, _I64, _I64]),

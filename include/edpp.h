@@ -190,6 +190,25 @@ int edpp_stream_add_i32(const int32_t *a, const int32_t *b, int32_t *c,
 int edpp_stream_triad_i32(const int32_t *a, const int32_t *b, int32_t *c,
                           int32_t s, int64_t n, void *stream);
 
+/* ---- allocation-free scan ------------------------------------------------ */
+
+/* Exclusive int32 look-back scan that allocates nothing and takes no
+ * workspace.  It has no counterpart in the reference; it exists for callers
+ * that cannot allocate device memory at the point of the call (host
+ * callbacks, real-time loops that must not touch the allocator, plugins whose
+ * host owns all device allocations).  Its scratch is one 1 MiB array in device
+ * global memory that every GPU loading the library holds until exit, so
+ * length is limited to edpp_scan_exclusive_i32_noalloc_max_length()
+ * (536,739,840 elements); longer inputs return EDPP_EINVAL.  The first call on
+ * a device looks up the array's device address (once per device; make that
+ * first call before any stream capture).  All calls share the one array:
+ * calls whose work overlaps on the GPU (different streams, or several host
+ * threads without ordering) race and give wrong results; order them on one
+ * stream.  Results equal edpp_scan_exclusive_i32 with EDPP_SCAN_LOOKBACK. */
+int edpp_scan_exclusive_i32_noalloc(const int32_t *in, int32_t *out, int64_t length,
+                                    void *stream);
+int64_t edpp_scan_exclusive_i32_noalloc_max_length(void);
+
 /* ---- bounded-wait self-test --------------------------------------------- */
 
 /* Runs a look-back scan over `length` int32 elements whose first tile is
