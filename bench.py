@@ -64,8 +64,13 @@ def call_bytes(name, n):
     return n * (GS_BYTES if name in ("gather", "scatter") else STREAM_BYTES[name])
 
 
-def call_launches(name, p):
-    return p if name in ("gather", "scatter") else 1
+def call_launches(name, p, method="partition"):
+    """Kernels of this library one call launches."""
+    if name not in ("gather", "scatter"):
+        return 1
+    if method == "sweep" or p == 1:
+        return p
+    return 5 if name == "gather" else 4  # count, bases, partition, (fetch,) apply
 
 
 def measured_peak_gbs():
@@ -265,6 +270,10 @@ def main(argv=None):
     ap.add_argument("--cpu-sample", type=int, default=1 << 26)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--method", default="partition", choices=["partition", "sweep"],
+                    help="gather/scatter schedule of the timed step")
+    ap.add_argument("--no-compare", action="store_true",
+                    help="skip timing the other gather/scatter schedule")
     args = ap.parse_args(argv)
     args.warmup = max(args.warmup, 3)
 
@@ -292,18 +301,21 @@ def main(argv=None):
     d_b = torch.from_numpy(h_b).to(dev)
     d_out = torch.empty(n, dtype=torch.int32, device=dev)
     d_fout = torch.empty(n, dtype=torch.float32, device=dev)
+    # one workspace serves every pass count (allocated outside the timed region)
+    ws = edpp.workspace(max(edpp.gs_workspace_bytes(k, n, p) for k in ("gather", "scatter")
+                            for p in PASSES), dev)
 
-    def run_call(name, p):
+    def run_call(name, p, method=args.method):
         if name == "gather":
-            edpp.gather(d_in, d_loc, p, out=d_out)
+            edpp.gather(d_in, d_loc, p, out=d_out, method=method, ws=ws)
         elif name == "scatter":
-            edpp.scatter(d_in, d_loc, p, out=d_out)
+            edpp.scatter(d_in, d_loc, p, out=d_out, method=method, ws=ws)
         else:
             edpp.stream(name, d_a, d_b, 3.0, out=d_fout)
 
     calls = step_calls()
     step_bytes = sum(call_bytes(name, n) for name, _ in calls)
-    launches_per_step = sum(call_launches(name, p) for name, p in calls)
+    launches_per_step = sum(call_launches(name, p, args.method) for name, p in calls)
 
     for _ in range(args.warmup):
         for c in calls:
@@ -349,9 +361,9 @@ def main(argv=None):
                            "frac_of_hbm": round(gbs / peak, 4)}
     dom = max(per_call_ms, key=lambda c: per_call_ms[c])
     dom_name = f"{dom[0]}_p{dom[1]}" if dom[1] else dom[0]
-    dom_launch_ms = per_call_ms[dom] / call_launches(*dom)
-    dom_bytes_per_launch = call_bytes(dom[0], n) / call_launches(*dom)
-    achieved = dom_bytes_per_launch / (dom_launch_ms * 1e-3) / 1e9
+    # The dominant call of the step: its algorithmic bytes over its CUDA-event
+    # duration (all launches of the call, which run back to back on the stream).
+    achieved = call_bytes(dom[0], n) / (per_call_ms[dom] * 1e-3) / 1e9
     traffic = None
     tf = ROOT / "profiles" / "traffic.json"
     if tf.exists():
@@ -361,9 +373,30 @@ def main(argv=None):
             traffic = None
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic,
-                "kernel": f"{dom_name} ({'pass_vec_kernel' if dom[1] else 'stream_vec_kernel'})",
+                "kernel": dom_name,
+                "launches_per_call": call_launches(dom[0], dom[1], args.method),
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"
                 if peak_kind == "measured" else "fallback 6.8 TB/s"}
+
+    # ---- the other schedule, per call, for comparison (not in `value`) ------
+    compare = None
+    if not args.no_compare:
+        other = "sweep" if args.method == "partition" else "partition"
+        compare = {"method": other}
+        for c in calls:
+            if c[0] not in ("gather", "scatter"):
+                continue
+            run_call(*c, method=other)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(args.steps):
+                run_call(*c, method=other)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / args.steps
+            compare[f"{c[0]}_p{c[1]}"] = {"ms": round(ms, 4),
+                                          "GB/s": round(call_bytes(c[0], n) / (ms * 1e-3) / 1e9, 1)}
 
     # ---- end to end: host buffers through the C ABI ------------------------
     e2e = None
@@ -422,7 +455,9 @@ def main(argv=None):
                                    "(2^28 f32, scalar 3.0)",
                        "n": n, "passes": list(PASSES), "parallelism": f"replicas{world}",
                        "l2": "inputs (1 GiB each) larger than L2; no flush"},
+            "gather_scatter_method": args.method,
             "primitives": primitives,
+            "compare": compare,
             "roofline": roofline,
             "gpu_launches": launches_per_step * args.steps,
             "clocks": clk.summary(),

@@ -1,0 +1,501 @@
+// gather_scatter_part.cu — partitioned multi-pass gather and scatter.
+//
+// Same results as the windowed passes of gather_scatter.cu (and of the
+// reference's gatherImpl.cpp:38-53 / scatterImpl.cpp:39-52), scheduled for
+// GB300's memory system.  On a random permutation of 2^28 int32 the direct
+// passes are bound by DRAM random access: every missed 4-byte load pulls
+// 64-128 bytes from DRAM and every 4-byte store to a sector not in L2 costs a
+// fill read plus a sector write.  Here the pass windows become partitions:
+//
+//   count      valid indices per window (P windows of W = 2^k elements)
+//   bases      exclusive scan of the counts -> write cursor of each window
+//   partition  each block stages a tile, groups its (index, payload) pairs
+//              by window in shared memory and appends one contiguous run per
+//              window at the window's cursor (coalesced 8-byte pairs)
+//   scatter:   apply  — pairs are consumed in window order through an atomic
+//              chunk ticket, so all SMs work inside one window at a time and
+//              the random stores land in an L2-resident slice of out[]
+//   gather:    fetch  — the same ordered sweep reads in[] inside an
+//              L2-resident window and regroups (i, value) by destination
+//              window (capacity W each: every i occurs once);
+//              apply  — ordered sweep over destination windows, out[i] = v
+//
+// Traffic per element: scatter 32 B, gather 48 B, nearly all streaming,
+// against 12 B algorithmic.  Indices outside [0,n) are dropped at `count`
+// and `partition`, as every pass of the windowed form skips them.  Scatter
+// with repeated destinations keeps one of the colliding values (unspecified
+// which), as the reference's racing stores do.
+#include <mutex>
+
+#include "common.cuh"
+
+namespace edpp {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kPer = 16;                    // elements per thread per tile
+constexpr int kTile = kThreads * kPer;      // 4096
+constexpr int kMaxWin = 2048;               // windows
+constexpr int64_t kMinWin = 1024;           // elements per window, at least
+constexpr int kChunk = 8192;                // pairs per ticket in ordered sweeps
+constexpr size_t kHdr = 256;                // tickets
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+__device__ __forceinline__ int ld_nc(const int32_t *p) {
+  int v;
+  asm volatile("ld.global.nc.L1::no_allocate.b32 %0, [%1];" : "=r"(v) : "l"(p));
+  return v;
+}
+
+// Rank of this lane's element among the tile's elements of window w
+// (-1: invalid), by warp-aggregated shared-memory atomics.
+__device__ __forceinline__ int rank_in_window(int w, uint32_t *scnt, unsigned lt) {
+  const unsigned peers = __match_any_sync(0xffffffffu, w);
+  const int leader = __ffs(peers) - 1;
+  uint32_t base = 0;
+  if (w >= 0 && (peers & lt) == 0u) base = atomicAdd(&scnt[w], static_cast<uint32_t>(__popc(peers)));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  return w >= 0 ? static_cast<int>(base) + __popc(peers & lt) : -1;
+}
+
+// Block-wide exclusive scan of scnt[0..nwin) into soff[], returns total.
+__device__ __forceinline__ uint32_t block_scan_counts(const uint32_t *scnt, uint32_t *soff, int nwin,
+                                                      uint32_t *s_warp) {
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int per = (nwin + kThreads - 1) / kThreads;
+  const int lo = min(nwin, tid * per), hi = min(nwin, lo + per);
+  uint32_t s = 0;
+  for (int i = lo; i < hi; ++i) s += scnt[i];
+  uint32_t incl = s;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d) incl += y;
+  }
+  if (lane == 31) s_warp[wid] = incl;
+  __syncthreads();
+  if (wid == 0) {
+    const uint32_t x = lane < kThreads / 32 ? s_warp[lane] : 0u;
+    uint32_t xi = x;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, xi, d);
+      if (lane >= d) xi += y;
+    }
+    if (lane < kThreads / 32) s_warp[lane] = xi - x;
+    if (lane == 31) s_warp[8] = xi;  // total (kThreads / 32 == 8 warps)
+  }
+  __syncthreads();
+  uint32_t run = s_warp[wid] + (incl - s);
+  for (int i = lo; i < hi; ++i) {
+    soff[i] = run;
+    run += scnt[i];
+  }
+  const uint32_t total = s_warp[8];
+  __syncthreads();
+  return total;
+}
+
+// ---- count ----------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads)
+    part_count_kernel(const int32_t *__restrict__ loc, int64_t n, int log_w, int nwin,
+                      uint32_t *__restrict__ cnt, bool vec) {
+  extern __shared__ uint32_t scnt[];
+  for (int i = threadIdx.x; i < nwin; i += kThreads) scnt[i] = 0;
+  __syncthreads();
+  const unsigned lt = lanemask_lt();
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * kThreads;
+  auto one = [&](int32_t l, bool in_range) {
+    const bool valid = in_range && static_cast<uint64_t>(static_cast<uint32_t>(l)) <
+                                       static_cast<uint64_t>(n) && l >= 0;
+    rank_in_window(valid ? (l >> log_w) : -1, scnt, lt);
+  };
+  if (vec) {
+    const int64_t n4 = n >> 2;
+    const int4 *l4 = reinterpret_cast<const int4 *>(loc);
+    // Trip count is uniform across the warp (rounded up), lanes past the end
+    // contribute invalid elements, so __match_any_sync sees the full warp.
+    const int64_t base0 = static_cast<int64_t>(blockIdx.x) * kThreads;
+    for (int64_t b = base0; b < n4; b += stride) {
+      const int64_t i = b + threadIdx.x;
+      int4 q = make_int4(-1, -1, -1, -1);
+      const bool ok = i < n4;
+      if (ok) q = __ldcs(l4 + i);
+      one(q.x, ok);
+      one(q.y, ok);
+      one(q.z, ok);
+      one(q.w, ok);
+    }
+    // tail
+    if (blockIdx.x == 0) {
+      const int64_t i = 4 * n4 + threadIdx.x;
+      const bool ok = threadIdx.x < 32 && i < n;
+      if (threadIdx.x < 32) one(ok ? loc[i] : -1, ok);
+    }
+  } else {
+    const int64_t base0 = static_cast<int64_t>(blockIdx.x) * kThreads;
+    for (int64_t b = base0; b < n; b += stride) {
+      const int64_t i = b + threadIdx.x;
+      const bool ok = i < n;
+      one(ok ? loc[i] : -1, ok);
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nwin; i += kThreads)
+    if (scnt[i]) atomicAdd(&cnt[i], scnt[i]);
+}
+
+// ---- bases: fill[w] = sum of cnt[0..w); fill2[w] = w * W (gather) ------------------
+__global__ void __launch_bounds__(kThreads)
+    part_bases_kernel(const uint32_t *cnt, uint32_t *fill, uint32_t *fill2, int nwin, int64_t w_elems,
+                      uint32_t *total) {
+  __shared__ uint32_t scnt[kMaxWin], soff[kMaxWin], s_warp[16];
+  for (int i = threadIdx.x; i < nwin; i += kThreads) scnt[i] = cnt[i];
+  __syncthreads();
+  const uint32_t t = block_scan_counts(scnt, soff, nwin, s_warp);
+  for (int i = threadIdx.x; i < nwin; i += kThreads) {
+    fill[i] = soff[i];
+    if (fill2) fill2[i] = static_cast<uint32_t>(static_cast<int64_t>(i) * w_elems);
+  }
+  if (threadIdx.x == 0) *total = t;
+}
+
+// Group the block's pairs by window and append one run per window at the
+// window's global cursor.  pair.x determines the window (x >> log_w); w[e] is
+// -1 for dropped elements; rank[e] from rank_in_window.
+template <int PER>
+__device__ __forceinline__ void flush_runs(const int2 (&pr)[PER], const int (&w)[PER],
+                                           const int (&rank)[PER], int nwin, int log_w,
+                                           uint32_t *scnt, uint32_t *soff, uint32_t *sgb,
+                                           uint32_t *s_warp, int2 *stage, uint32_t *fill,
+                                           int2 *__restrict__ dst) {
+  const uint32_t total = block_scan_counts(scnt, soff, nwin, s_warp);
+  for (int i = threadIdx.x; i < nwin; i += kThreads)
+    if (scnt[i]) sgb[i] = atomicAdd(&fill[i], scnt[i]);
+#pragma unroll
+  for (int e = 0; e < PER; ++e)
+    if (w[e] >= 0) stage[soff[w[e]] + rank[e]] = pr[e];
+  __syncthreads();
+  for (uint32_t s = threadIdx.x; s < total; s += kThreads) {
+    const int2 p = stage[s];
+    const int ww = p.x >> log_w;
+    dst[sgb[ww] + (s - soff[ww])] = p;
+  }
+}
+
+// ---- partition -------------------------------------------------------------------
+// Gather pairs {loc, i}; scatter pairs {loc, in[i]}.
+template <bool kScatter>
+__global__ void __launch_bounds__(kThreads)
+    part_partition_kernel(const int32_t *__restrict__ loc, const int32_t *__restrict__ in, int64_t n,
+                          int log_w, int nwin, uint32_t *__restrict__ fill, int2 *__restrict__ pairs,
+                          bool vec) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  int2 *stage = reinterpret_cast<int2 *>(smem);
+  uint32_t *scnt = reinterpret_cast<uint32_t *>(stage + kTile);
+  uint32_t *soff = scnt + nwin;
+  uint32_t *sgb = soff + nwin;
+  __shared__ uint32_t s_warp[16];
+  for (int i = threadIdx.x; i < nwin; i += kThreads) scnt[i] = 0;
+  __syncthreads();
+  const int64_t base = static_cast<int64_t>(blockIdx.x) * kTile;
+  const int t = threadIdx.x;
+  const unsigned lt = lanemask_lt();
+  int2 pr[kPer];
+  int w[kPer], rank[kPer];
+#pragma unroll
+  for (int k = 0; k < kPer / 4; ++k) {
+    const int64_t i0 = base + static_cast<int64_t>(k * kThreads + t) * 4;  // 4 elements
+    int4 l = make_int4(-1, -1, -1, -1), v = make_int4(0, 0, 0, 0);
+    if (vec && i0 + 3 < n) {
+      l = __ldcs(reinterpret_cast<const int4 *>(loc + i0));
+      if (kScatter) v = __ldcs(reinterpret_cast<const int4 *>(in + i0));
+    } else {
+      if (i0 + 0 < n) { l.x = loc[i0 + 0]; if (kScatter) v.x = in[i0 + 0]; }
+      if (i0 + 1 < n) { l.y = loc[i0 + 1]; if (kScatter) v.y = in[i0 + 1]; }
+      if (i0 + 2 < n) { l.z = loc[i0 + 2]; if (kScatter) v.z = in[i0 + 2]; }
+      if (i0 + 3 < n) { l.w = loc[i0 + 3]; if (kScatter) v.w = in[i0 + 3]; }
+    }
+    const int32_t ls[4] = {l.x, l.y, l.z, l.w};
+    const int32_t vs[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int e = 4 * k + q;
+      const bool valid = (i0 + q < n) && ls[q] >= 0 && static_cast<int64_t>(ls[q]) < n;
+      w[e] = valid ? (ls[q] >> log_w) : -1;
+      pr[e] = make_int2(ls[q], kScatter ? vs[q] : static_cast<int32_t>(i0 + q));
+      rank[e] = rank_in_window(w[e], scnt, lt);
+    }
+  }
+  __syncthreads();
+  flush_runs<kPer>(pr, w, rank, nwin, log_w, scnt, soff, sgb, s_warp, stage, fill, pairs);
+}
+
+// ---- gather fetch: ordered sweep, v = in[loc], regroup by destination --------------
+__global__ void __launch_bounds__(kThreads)
+    part_fetch_kernel(const int2 *__restrict__ pairs, const uint32_t *__restrict__ total_p,
+                      const int32_t *__restrict__ in, int log_w, int nwin,
+                      uint32_t *__restrict__ fill2, int2 *__restrict__ pairs2,
+                      unsigned long long *ticket) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  int2 *stage = reinterpret_cast<int2 *>(smem);
+  uint32_t *scnt = reinterpret_cast<uint32_t *>(stage + kTile);
+  uint32_t *soff = scnt + nwin;
+  uint32_t *sgb = soff + nwin;
+  __shared__ uint32_t s_warp[16];
+  __shared__ int64_t s_chunk;
+  const int64_t total = *total_p;
+  const unsigned lt = lanemask_lt();
+  const int t = threadIdx.x;
+  while (true) {
+    if (t == 0) s_chunk = static_cast<int64_t>(atomicAdd(ticket, 1ull));
+    for (int i = t; i < nwin; i += kThreads) scnt[i] = 0;
+    __syncthreads();
+    const int64_t base = s_chunk * kTile;
+    if (base >= total) break;
+    int2 pr[kPer];
+    int w[kPer], rank[kPer];
+    // Pairs, 2 per 16-byte vector, row-striped; random loads all in flight.
+    int2 src[kPer];
+#pragma unroll
+    for (int k = 0; k < kPer / 2; ++k) {
+      const int64_t j = base + static_cast<int64_t>(k * kThreads + t) * 2;
+      int4 q = make_int4(-1, 0, -1, 0);
+      if (j + 1 < total) q = __ldcs(reinterpret_cast<const int4 *>(pairs + j));
+      else if (j < total) { const int2 a = pairs[j]; q.x = a.x; q.y = a.y; }
+      src[2 * k] = make_int2(q.x, q.y);
+      src[2 * k + 1] = make_int2(q.z, q.w);
+    }
+#pragma unroll
+    for (int e = 0; e < kPer; ++e) {
+      const bool valid = src[e].x >= 0;
+      pr[e] = make_int2(src[e].y, valid ? ld_nc(in + src[e].x) : 0);  // {i, value}
+    }
+#pragma unroll
+    for (int e = 0; e < kPer; ++e) {
+      w[e] = src[e].x >= 0 ? (pr[e].x >> log_w) : -1;
+      rank[e] = rank_in_window(w[e], scnt, lt);
+    }
+    __syncthreads();
+    flush_runs<kPer>(pr, w, rank, nwin, log_w, scnt, soff, sgb, s_warp, stage, fill2, pairs2);
+    __syncthreads();
+  }
+}
+
+// ---- apply: ordered sweep, out[p.x] = p.y ------------------------------------------
+// Scatter: pairs [0, total).  Gather: destination window j holds
+// [j*W, fill2[j]).  chunks_per_win == 0 means the flat scatter layout.
+__global__ void __launch_bounds__(kThreads)
+    part_apply_kernel(const int2 *__restrict__ pairs, const uint32_t *__restrict__ total_p,
+                      const uint32_t *__restrict__ fill2, int64_t w_elems, int64_t chunks_per_win,
+                      int64_t num_chunks, int32_t *__restrict__ out, unsigned long long *ticket) {
+  __shared__ int64_t s_chunk;
+  const int t = threadIdx.x;
+  while (true) {
+    if (t == 0) s_chunk = static_cast<int64_t>(atomicAdd(ticket, 1ull));
+    __syncthreads();
+    const int64_t c = s_chunk;
+    __syncthreads();
+    if (c >= num_chunks) break;
+    int64_t lo, hi;
+    if (chunks_per_win == 0) {
+      lo = c * kChunk;
+      hi = min64(lo + kChunk, static_cast<int64_t>(*total_p));
+    } else {
+      const int64_t j = c / chunks_per_win, k = c % chunks_per_win;
+      lo = j * w_elems + k * kChunk;
+      hi = min64(lo + kChunk, static_cast<int64_t>(fill2[j]));
+    }
+    // 2 pairs per vector, 4 vectors per thread in flight.
+    for (int64_t j0 = lo + 2 * t; j0 < hi; j0 += 2 * kThreads * 4) {
+      int4 q[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int64_t j = j0 + static_cast<int64_t>(u) * 2 * kThreads;
+        q[u] = make_int4(-1, 0, -1, 0);
+        if (j + 1 < hi) q[u] = __ldcs(reinterpret_cast<const int4 *>(pairs + j));
+        else if (j < hi) { const int2 a = pairs[j]; q[u].x = a.x; q[u].y = a.y; }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        if (q[u].x >= 0) out[q[u].x] = q[u].y;
+        if (q[u].z >= 0) out[q[u].z] = q[u].w;
+      }
+    }
+  }
+}
+
+// ---- host side ---------------------------------------------------------------------
+struct Plan {
+  int log_w = 0;
+  int nwin = 0;
+  int64_t w_elems = 0;
+};
+
+int l2_bytes() {
+  static std::once_flag once;
+  static int bytes = 126 << 20;
+  std::call_once(once, [] {
+    int dev = 0, v = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&v, cudaDevAttrL2CacheSize, dev) == cudaSuccess && v > 0)
+      bytes = v;
+  });
+  return bytes;
+}
+
+// Windows of W = 2^k elements.  pass >= 2: W = next power of two >= ceil(n/pass);
+// pass == 0: the largest W whose int32 slice fills at most half of L2.
+Plan make_plan(int64_t n, int pass) {
+  Plan p;
+  int64_t w;
+  if (pass <= 0) {
+    w = 1;
+    while (w * 2 * 4 <= l2_bytes() / 2) w *= 2;
+  } else {
+    const int64_t want = (n + pass - 1) / pass;
+    w = 1;
+    while (w < want) w *= 2;
+  }
+  if (w < kMinWin) w = kMinWin;  // keeps window starts 16-byte aligned in pairs2
+  while ((n + w - 1) / w > kMaxWin) w *= 2;
+  p.w_elems = w;
+  p.log_w = 0;
+  while ((int64_t(1) << p.log_w) < w) ++p.log_w;
+  p.nwin = static_cast<int>((n + w - 1) / w);
+  if (p.nwin < 1) p.nwin = 1;
+  return p;
+}
+
+struct Layout {
+  size_t cnt, fill, fill2, total, pairs, pairs2, bytes;
+};
+
+Layout layout_of(int64_t n, const Plan &p, bool gather) {
+  Layout L{};
+  size_t o = kHdr;
+  auto take = [&](size_t b) {
+    const size_t at = o;
+    o += round_up(b, 256);
+    return at;
+  };
+  L.cnt = take(4 * static_cast<size_t>(p.nwin));
+  L.total = take(16);
+  L.fill = take(4 * static_cast<size_t>(p.nwin));
+  L.fill2 = gather ? take(4 * static_cast<size_t>(p.nwin)) : 0;
+  L.pairs = take(8 * static_cast<size_t>(n));
+  L.pairs2 = gather ? take(8 * static_cast<size_t>(p.nwin) * static_cast<size_t>(p.w_elems)) : 0;
+  L.bytes = o;
+  return L;
+}
+
+size_t part_smem(int nwin) { return static_cast<size_t>(kTile) * 8 + 3 * 4 * static_cast<size_t>(nwin); }
+
+template <typename K> int set_smem(K kernel) {
+  const size_t bytes = part_smem(kMaxWin);
+  return cuda_status(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          static_cast<int>(bytes)));
+}
+
+int ensure_attrs() {
+  static std::once_flag once[64];
+  static int st[64];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  std::call_once(once[dev], [] {
+    int d = 0;
+    cudaGetDevice(&d);
+    if (d < 0 || d >= 64) d = 0;
+    int s = set_smem(part_partition_kernel<false>);
+    if (s == EDPP_OK) s = set_smem(part_partition_kernel<true>);
+    if (s == EDPP_OK) s = set_smem(part_fetch_kernel);
+    st[d] = s;
+  });
+  return st[dev];
+}
+
+template <bool kScatter>
+int part_run(const int32_t *in, int32_t *out, int64_t n, const int32_t *loc, int pass, void *ws,
+             size_t ws_bytes, void *stream) {
+  if (n < 0 || pass < 0) return EDPP_EINVAL;
+  if (n == 0) return EDPP_OK;
+  if (!in || !out || !loc) return EDPP_EINVAL;
+  if (n > INT32_MAX) return EDPP_EINVAL;
+  if (pass == 1) {  // one window: the direct single sweep is the partition
+    return kScatter ? edpp_scatter_i32(in, out, n, loc, 1, stream)
+                    : edpp_gather_i32(in, out, n, loc, 1, stream);
+  }
+  const Plan p = make_plan(n, pass);
+  const Layout L = layout_of(n, p, !kScatter);
+  if (!ws || ws_bytes < L.bytes) return EDPP_ENOMEM;
+  int s = ensure_attrs();
+  if (s != EDPP_OK) return s;
+  cudaStream_t st = as_stream(stream);
+  char *w = static_cast<char *>(ws);
+  auto *tickets = reinterpret_cast<unsigned long long *>(w);
+  auto *cnt = reinterpret_cast<uint32_t *>(w + L.cnt);
+  auto *total = reinterpret_cast<uint32_t *>(w + L.total);
+  auto *fill = reinterpret_cast<uint32_t *>(w + L.fill);
+  auto *fill2 = kScatter ? nullptr : reinterpret_cast<uint32_t *>(w + L.fill2);
+  auto *pairs = reinterpret_cast<int2 *>(w + L.pairs);
+  auto *pairs2 = kScatter ? nullptr : reinterpret_cast<int2 *>(w + L.pairs2);
+  if (cudaMemsetAsync(w, 0, L.fill, st) != cudaSuccess) return EDPP_ECUDA;  // tickets, cnt, total
+
+  const int sms = device_sm_count();
+  const bool vec_loc = aligned16(loc);
+  const bool vec = vec_loc && (!kScatter || aligned16(in));
+  const int64_t count_blocks = min64(static_cast<int64_t>(sms) * 8, (n + 4 * kThreads - 1) / (4 * kThreads));
+  part_count_kernel<<<static_cast<unsigned>(max64(count_blocks, 1)), kThreads, 4 * p.nwin, st>>>(
+      loc, n, p.log_w, p.nwin, cnt, vec_loc);
+  part_bases_kernel<<<1, kThreads, 0, st>>>(cnt, fill, fill2, p.nwin, p.w_elems, total);
+  const int64_t tiles = (n + kTile - 1) / kTile;
+  const size_t smem = part_smem(p.nwin);
+  part_partition_kernel<kScatter><<<static_cast<unsigned>(tiles), kThreads, smem, st>>>(
+      loc, in, n, p.log_w, p.nwin, fill, pairs, vec);
+  const unsigned persist = static_cast<unsigned>(sms) * 4;
+  if (kScatter) {
+    const int64_t chunks = (n + kChunk - 1) / kChunk;  // upper bound; total <= n
+    part_apply_kernel<<<persist, kThreads, 0, st>>>(pairs, total, nullptr, 0, 0, chunks, out,
+                                                    tickets + 1);
+  } else {
+    part_fetch_kernel<<<persist, kThreads, smem, st>>>(pairs, total, in, p.log_w, p.nwin, fill2,
+                                                       pairs2, tickets);
+    const int64_t cpw = (p.w_elems + kChunk - 1) / kChunk;
+    part_apply_kernel<<<persist, kThreads, 0, st>>>(pairs2, total, fill2, p.w_elems, cpw,
+                                                    cpw * p.nwin, out, tickets + 1);
+  }
+  return launch_status();
+}
+
+}  // namespace
+}  // namespace edpp
+
+extern "C" {
+
+size_t edpp_gather_workspace_size(int64_t length, int pass) {
+  if (length <= 0 || pass < 0 || pass == 1) return 0;
+  return edpp::layout_of(length, edpp::make_plan(length, pass), true).bytes;
+}
+
+size_t edpp_scatter_workspace_size(int64_t length, int pass) {
+  if (length <= 0 || pass < 0 || pass == 1) return 0;
+  return edpp::layout_of(length, edpp::make_plan(length, pass), false).bytes;
+}
+
+int edpp_gather_i32_ws(const int32_t *in, int32_t *out, int64_t length, const int32_t *loc,
+                       int pass, void *ws, size_t ws_bytes, void *stream) {
+  return edpp::part_run<false>(in, out, length, loc, pass, ws, ws_bytes, stream);
+}
+
+int edpp_scatter_i32_ws(const int32_t *in, int32_t *out, int64_t length, const int32_t *loc,
+                        int pass, void *ws, size_t ws_bytes, void *stream) {
+  return edpp::part_run<true>(in, out, length, loc, pass, ws, ws_bytes, stream);
+}
+
+}  // extern "C"

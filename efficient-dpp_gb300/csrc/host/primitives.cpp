@@ -67,12 +67,24 @@ double split_any(const int *d_in, int *d_out, int *d_start, int length, int buck
 
 }  // namespace
 
+// Multi-pass gather / scatter through the partitioned form (same results as
+// the reference's pass-by-pass sweeps, pass windows realised as partitions).
 double gather(const int *d_in, int *d_out, int length, const int *d_loc, int, int, int pass) {
-  return timed([&] { return edpp_gather_i32(d_in, d_out, length, d_loc, pass, nullptr); });
+  if (pass < 1) return -1;
+  Temp ws(edpp_gather_workspace_size(length, pass));
+  if (!ws.ok()) return -1;
+  return timed([&] {
+    return edpp_gather_i32_ws(d_in, d_out, length, d_loc, pass, ws.p, ws.bytes, nullptr);
+  });
 }
 
 double scatter(const int *d_in, int *d_out, int length, const int *d_loc, int, int, int pass) {
-  return timed([&] { return edpp_scatter_i32(d_in, d_out, length, d_loc, pass, nullptr); });
+  if (pass < 1) return -1;
+  Temp ws(edpp_scatter_workspace_size(length, pass));
+  if (!ws.ok()) return -1;
+  return timed([&] {
+    return edpp_scatter_i32_ws(d_in, d_out, length, d_loc, pass, ws.p, ws.bytes, nullptr);
+  });
 }
 
 double scan_chained(const int *d_in, int *d_out, int length, int, int, int R, int L) {

@@ -42,6 +42,10 @@ SIGNATURES = {
     "edpp_device_fault": (_I, [ctypes.POINTER(ctypes.c_uint), _I]),
     "edpp_gather_i32": (_I, [_VP, _VP, _I64, _VP, _I, _VP]),
     "edpp_scatter_i32": (_I, [_VP, _VP, _I64, _VP, _I, _VP]),
+    "edpp_gather_workspace_size": (_SZ, [_I64, _I]),
+    "edpp_scatter_workspace_size": (_SZ, [_I64, _I]),
+    "edpp_gather_i32_ws": (_I, [_VP, _VP, _I64, _VP, _I, _VP, _SZ, _VP]),
+    "edpp_scatter_i32_ws": (_I, [_VP, _VP, _I64, _VP, _I, _VP, _SZ, _VP]),
     "edpp_scan_workspace_size": (_SZ, [_I64, _I, _I]),
     "edpp_scan_exclusive_i32": (_I, [_VP, _VP, _I64, _I, _VP, _SZ, _VP]),
     "edpp_scan_inclusive_i32": (_I, [_VP, _VP, _I64, _I, _VP, _SZ, _VP]),
@@ -144,30 +148,45 @@ def sync_status(clear: bool = True) -> int:
 
 # ---------------------------------------------------------------------------
 # primitives
-def gather(inp, loc, passes: int = 1, out=None):
+def _gs(kind, inp, loc, passes, out, method, ws):
     torch = _torch()
     _cuda_tensor(inp, torch.int32, "inp")
     _cuda_tensor(loc, torch.int32, "loc")
     n = loc.numel()
-    if inp.numel() < n:
+    if kind == "gather" and inp.numel() < n:
         raise ValueError("inp shorter than loc")
     if out is None:
         out = torch.zeros(n, dtype=torch.int32, device=loc.device)
-    check(lib().edpp_gather_i32(_p(inp), _p(out), n, _p(loc), int(passes),
-                                current_stream_handle()), "gather")
+    st = current_stream_handle()
+    if method == "sweep":
+        f = lib().edpp_gather_i32 if kind == "gather" else lib().edpp_scatter_i32
+        check(f(_p(inp), _p(out), n, _p(loc), int(passes), st), kind)
+    elif method == "partition":
+        need = gs_workspace_bytes(kind, n, passes)
+        if ws is None:
+            ws = workspace(need, loc.device)
+        f = lib().edpp_gather_i32_ws if kind == "gather" else lib().edpp_scatter_i32_ws
+        check(f(_p(inp), _p(out), n, _p(loc), int(passes), _p(ws), ws.numel(), st), kind)
+    else:
+        raise ValueError(method)
     return out
 
 
-def scatter(inp, loc, passes: int = 1, out=None):
-    torch = _torch()
-    _cuda_tensor(inp, torch.int32, "inp")
-    _cuda_tensor(loc, torch.int32, "loc")
-    n = loc.numel()
-    if out is None:
-        out = torch.zeros(n, dtype=torch.int32, device=loc.device)
-    check(lib().edpp_scatter_i32(_p(inp), _p(out), n, _p(loc), int(passes),
-                                 current_stream_handle()), "scatter")
-    return out
+def gs_workspace_bytes(kind: str, n: int, passes: int) -> int:
+    f = lib().edpp_gather_workspace_size if kind == "gather" else lib().edpp_scatter_workspace_size
+    return f(int(n), int(passes))
+
+
+def gather(inp, loc, passes: int = 1, out=None, method: str = "sweep", ws=None):
+    """out[i] = inp[loc[i]].  method "sweep": one launch per pass window, each
+    reading all of loc (the reference's schedule); "partition": the windows
+    as partitions (passes=0 sizes them to L2)."""
+    return _gs("gather", inp, loc, passes, out, method, ws)
+
+
+def scatter(inp, loc, passes: int = 1, out=None, method: str = "sweep", ws=None):
+    """out[loc[i]] = inp[i]; methods as gather."""
+    return _gs("scatter", inp, loc, passes, out, method, ws)
 
 
 _SCAN_FN = {

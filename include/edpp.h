@@ -116,6 +116,24 @@ int edpp_gather_i32(const int32_t *in, int32_t *out, int64_t length,
 int edpp_scatter_i32(const int32_t *in, int32_t *out, int64_t length,
                      const int32_t *loc, int pass, void *stream);
 
+/* Partitioned multi-pass gather / scatter: identical results to
+ * edpp_gather_i32 / edpp_scatter_i32 for every pass count, with the pass
+ * windows realised as partitions.  Requests are grouped by window into a
+ * caller workspace (edpp_*_workspace_size), then each window's random side is
+ * served while that window of the array sits in L2.  pass >= 2: windows of
+ * the next power of two >= ceil(length/pass) elements; pass == 0: windows
+ * sized to half of this GPU's L2; pass == 1: the direct single sweep (no
+ * workspace).  A scatter with repeated destinations keeps one of the
+ * colliding values. */
+size_t edpp_gather_workspace_size(int64_t length, int pass);
+size_t edpp_scatter_workspace_size(int64_t length, int pass);
+int edpp_gather_i32_ws(const int32_t *in, int32_t *out, int64_t length,
+                       const int32_t *loc, int pass, void *ws, size_t ws_bytes,
+                       void *stream);
+int edpp_scatter_i32_ws(const int32_t *in, int32_t *out, int64_t length,
+                        const int32_t *loc, int pass, void *ws, size_t ws_bytes,
+                        void *stream);
+
 /* ---- global scan -------------------------------------------------------- */
 
 /* Bytes of workspace a scan of `length` elements of `dtype` with `algo`
