@@ -259,6 +259,200 @@ def run_reference(args, rank, world):
     return 0
 
 
+def run_batch_workload(args, rank, world):
+    """Config 5: 4096 uneven segments (scan / 64-bucket split / permutation
+    gather, total <= 2^30 int32): one persistent launch (CUDA graph) against
+    one plain C-ABI call per segment.  Metric: elements/s."""
+    import numpy as np
+    import torch
+
+    import edpp
+    from edpp import batch as B
+    edpp.lib()
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.set_device(dev)
+    segs = B.config5_segments()
+    in0, in1 = B.gen_inputs(segs, seed=4)
+    n = len(in0)
+    elems = int(segs["length"].sum())
+    nbytes = B.algorithmic_bytes(segs)
+    d0 = torch.from_numpy(in0).to(dev)
+    d1 = torch.from_numpy(in1).to(dev)
+    o0 = torch.zeros(n, dtype=torch.int32, device=dev)
+    o1 = torch.zeros(n, dtype=torch.int32, device=dev)
+    q0 = torch.zeros_like(o0)
+    q1 = torch.zeros_like(o1)
+    stream = torch.cuda.current_stream()
+
+    tuning = B.tuned(segs)
+    tune_info = None
+    if args.autotune:
+        plan0 = B.Plan(segs)
+        ws0 = plan0.workspace(dev)
+        tuning, tms = B.autotune(segs, d0, d1, o0, o1, ws0, reps=3)
+        B.record_tuning(segs, tuning, tms, {"segments": len(segs), "elements": elems})
+        tune_info = {"tuning": tuning.as_dict(), "ms": round(tms, 4)}
+        del ws0, plan0
+    plan = B.Plan(segs, tuning)
+    ws = plan.workspace(dev)
+    plan.upload(ws)
+    pws = B.plain_workspace(segs, dev)
+
+    def timed(fn, reps):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        barrier(world)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return max_over_ranks(e0.elapsed_time(e1) / reps, world)
+
+    plain_ms = timed(lambda: B.run_plain(segs, d0, d1, q0, q1, pws), args.steps)
+    # batched: capture one launch in a CUDA graph, replay it
+    g = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream()
+    side.wait_stream(stream)
+    with torch.cuda.stream(side):
+        with torch.cuda.graph(g):
+            plan.launch(d0, d1, o0, o1, ws)
+    stream.wait_stream(side)
+    with ClockSampler(int(dev.index or 0)) as clk:
+        batch_ms = timed(g.replay, args.steps)
+    stream_ms = timed(lambda: plan.launch(d0, d1, o0, o1, ws), args.steps)
+    identical = bool(torch.equal(o0, q0) and torch.equal(o1, q1))
+    if edpp.sync_status() != edpp.EDPP_OK:
+        raise SystemExit("device fault in the batch workload")
+    peak, peak_kind = measured_peak_gbs()
+    gbs = nbytes / (batch_ms * 1e-3) / 1e9
+    ops = {B.OP_NAMES[k]: int((segs["op"] == k).sum()) for k in (0, 1, 2)}
+    if rank == 0:
+        print(json.dumps({
+            "metric": METRIC, "workload_metric": "batched elements/s (one persistent launch) vs "
+                                                 "plain per-segment launches",
+            "value": round(world * elems / (batch_ms * 1e-3), 1), "unit": "elements/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(batch_ms, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+            "config": {"workload": "4096 segments, log-uniform 2^10..2^24 rescaled to <= 2^30 "
+                                   "int32 (seed 4), ops scan / 64-bucket split / gather",
+                       "segments": len(segs), "elements": elems, "ops": ops,
+                       "tasks": plan.num_tasks, "tuning": tuning.as_dict() if tuning else "default"},
+            "plain": {"ms": round(plain_ms, 4), "elements/s": round(elems / (plain_ms * 1e-3), 1)},
+            "batched_graph": {"ms": round(batch_ms, 4), "GB/s": round(gbs, 1),
+                              "frac_of_hbm": round(gbs / peak, 4)},
+            "batched_stream_launch_ms": round(stream_ms, 4),
+            "speedup_vs_plain": round(plain_ms / batch_ms, 3),
+            "identical_to_plain": identical,
+            "autotune": tune_info,
+            "roofline": {"bound": "hbm", "achieved": round(gbs, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(gbs / peak, 4), "traffic": None,
+                         "kernel": "batch_kernel (whole batch)",
+                         "peak_source": peak_kind},
+            "gpu_launches": 1 * args.steps,
+            "clocks": clk.summary(),
+        }), flush=True)
+    return 0
+
+
+def run_serve_workload(args, rank, world):
+    """Config 5, serving: Poisson arrivals at swept rates of requests with
+    log-uniform sizes 4K..64M elements (op scan / 64-bucket split / gather),
+    host buffers in pinned memory, admission cap 40 GB of HBM, continuous
+    batching; p50 / p99 latency (submit -> outputs in host memory)."""
+    import numpy as np
+    import torch
+
+    import edpp
+    from edpp import batch as B
+    from edpp import serve as S
+    edpp.lib()
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.set_device(dev)
+    if rank != 0:
+        return 0
+    npay = args.serve_payloads
+    sizes, ops = [], []
+    for i in range(npay):
+        u = (edpp.lib().edpp_gen_draw(4 ^ 0x5E, i) >> 11) * (1.0 / 9007199254740992.0)
+        sizes.append(int(2.0 ** (12 + 14 * u)))
+        ops.append(edpp.lib().edpp_gen_draw(4 ^ 0x5F, i) % 3)
+    segs = B.layout(sizes, ops, 64)
+    in0, in1 = B.gen_inputs(segs, seed=5)
+    total = len(in0)
+    p_in0, p_in1 = S.pinned_empty(total), S.pinned_empty(total)
+    p_o0, p_o1 = S.pinned_empty(total), S.pinned_empty(total)
+    p_in0[:] = in0
+    p_in1[:] = in1
+    pay = [(int(s["op"]), int(s["offset"]), int(s["length"])) for s in segs]
+    rng = np.random.default_rng(6)
+    results = []
+    srv = S.Server(pool_bytes=int(args.pool_gb * 1e9), slots=args.serve_slots)
+    # warm-up: every payload once
+    ids = [srv.submit(op, p_in0[o:o + L], p_in1[o:o + L], p_o0[o:o + L], p_o1[o:o + L], 64)
+           for op, o, L in pay]
+    for rid in ids:
+        st, _ = srv.wait(rid)
+        assert st == 0
+    with ClockSampler(int(dev.index or 0)) as clk:
+        for rate in [float(x) for x in args.rates.split(",")]:
+            n = args.serve_requests
+            gaps = rng.exponential(1.0 / rate, size=n)
+            arrivals = np.cumsum(gaps)
+            inflight = {}
+            lat, queue, elems = [], [], 0
+            t0 = time.perf_counter()
+            for i in range(n):
+                k = i % npay
+                if k in inflight:  # payload buffers still in use: wait for them
+                    st, tm = srv.wait(inflight.pop(k))
+                    assert st == 0
+                    lat.append(tm.latency_ms)
+                    queue.append(tm.queue_ms)
+                now = time.perf_counter() - t0
+                if arrivals[i] > now:
+                    time.sleep(arrivals[i] - now)
+                op, o, L = pay[k]
+                inflight[k] = srv.submit(op, p_in0[o:o + L], p_in1[o:o + L], p_o0[o:o + L],
+                                         p_o1[o:o + L], 64)
+                elems += L
+            for rid in inflight.values():
+                st, tm = srv.wait(rid)
+                assert st == 0
+                lat.append(tm.latency_ms)
+                queue.append(tm.queue_ms)
+            wall = time.perf_counter() - t0
+            lat = np.array(lat)
+            results.append({"rate_req_s": rate, "requests": n,
+                            "achieved_req_s": round(n / wall, 1),
+                            "elements/s": round(elems / wall, 1),
+                            "p50_ms": round(float(np.percentile(lat, 50)), 3),
+                            "p99_ms": round(float(np.percentile(lat, 99)), 3),
+                            "mean_ms": round(float(lat.mean()), 3),
+                            "queue_p99_ms": round(float(np.percentile(queue, 99)), 3)})
+    stats = srv.stats()
+    srv.close()
+    best = max(results, key=lambda r: r["elements/s"])
+    print(json.dumps({
+        "metric": METRIC, "workload_metric": "served elements/s with p50/p99 latency",
+        "value": best["elements/s"], "unit": "elements/s", "n_gpus": world,
+        "steps": len(results), "warmup": 1, "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": {"workload": "Poisson arrivals, sizes log-uniform 2^12..2^26 int32, ops scan / "
+                               "64-bucket split / gather, pinned host buffers",
+                   "payloads": npay, "pool_bytes": int(args.pool_gb * 1e9),
+                   "slots": args.serve_slots},
+        "rates": results, "server": stats, "clocks": clk.summary(),
+        "e2e": {"value": best["elements/s"], "unit": "elements/s",
+                "note": "every request copies inputs host->device and outputs back"},
+    }), flush=True)
+    return 0
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawTextHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -274,12 +468,27 @@ def main(argv=None):
                     help="gather/scatter schedule of the timed step")
     ap.add_argument("--no-compare", action="store_true",
                     help="skip timing the other gather/scatter schedule")
+    ap.add_argument("--workload", default="gs_stream", choices=["gs_stream", "batch", "serve"],
+                    help="gs_stream: multi-pass gather/scatter + STREAM (default); "
+                         "batch: 4096 uneven segments, batched vs plain; "
+                         "serve: Poisson request stream through the server")
+    ap.add_argument("--rates", default="100,300,1000,3000", help="serve: request rates (1/s)")
+    ap.add_argument("--serve-requests", type=int, default=400)
+    ap.add_argument("--serve-payloads", type=int, default=48)
+    ap.add_argument("--serve-slots", type=int, default=4)
+    ap.add_argument("--pool-gb", type=float, default=40.0)
+    ap.add_argument("--autotune", action="store_true",
+                    help="batch: run the autotuner and record its choice")
     args = ap.parse_args(argv)
     args.warmup = max(args.warmup, 3)
 
     rank, world, local = dist_setup()
     if args.impl == "reference":
         return run_reference(args, rank, world)
+    if args.workload == "batch":
+        return run_batch_workload(args, rank, world)
+    if args.workload == "serve":
+        return run_serve_workload(args, rank, world)
 
     import numpy as np
     import torch

@@ -1,0 +1,593 @@
+// batch.cu — many uneven segments of scan / stable split / permutation gather
+// in one persistent, work-queue-scheduled launch.
+//
+// The host planner (below) turns a segment table into a task queue.  Every
+// task is one tile of one segment:
+//   SCAN     exclusive int32 scan tile; tiles of a segment are chained by a
+//            decoupled look-back over the segment's own tile states
+//   GATHER   out0[i] = in0[in1[i]] for a tile, indices local to the segment
+//   HIST     bucket counts of a split tile -> column t of the segment's
+//            bucket-major histogram his[b*T + t]; the block that finishes a
+//            segment's last HIST tile scans that histogram in place and
+//            publishes the segment's ready flag (release)
+//   SPLIT    stable key/value scatter of a tile once the ready flag is set
+//            (acquire); same ranking as split.cu, 64-bucket-class tiles
+// Blocks take tasks from one atomic ticket in queue order.  A task waits only
+// on tasks earlier in the queue (look-back predecessors, its segment's HIST
+// tiles), which running blocks already hold, so the schedule always makes
+// progress; every wait is bounded by %globaltimer and reports
+// EDPP_FAULT_TIMEOUT instead of hanging.
+//
+// Tuning (edpp_batch_tuning, chosen per size class by edpp_batch_autotune):
+// blocks per SM of the persistent grid, how many segments a split's SPLIT
+// tasks are deferred behind its HIST tasks, and the segment order.
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <numeric>
+#include <vector>
+
+#include "batch_plan.h"
+#include "scan_tile.cuh"
+
+namespace edpp {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kChunks = 4;
+using TS32 = TileScan<int32_t, kThreads, kChunks>;
+constexpr int kTile = TS32::kTile;  // 4096 elements for every task kind
+static_assert(kTile == kBatchTile, "batch tile size");
+constexpr int kWarps = kThreads / 32;
+constexpr int kSeg = kTile / kWarps;  // 512 elements per warp in SPLIT
+constexpr int kIters = kSeg / 32;     // 16
+constexpr int kMaxB = kBatchMaxBuckets;
+
+enum TaskKind : int32_t { kTaskScan = 0, kTaskGather = 1, kTaskHist = 2, kTaskSplit = 3 };
+
+__device__ __forceinline__ unsigned lanemask_lt_b() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+union __align__(128) BatchSmem {
+  struct {
+    int32_t tile[kTile];
+    TS32::Shared sh;
+  } scan;
+  struct {
+    int32_t keys[kTile];
+    int32_t vals[kTile];
+    uint16_t cnt16[kWarps * kMaxB];
+    int32_t toff[kMaxB];
+    int32_t gofs[kMaxB];
+  } split;
+  struct {
+    uint32_t cnt[kMaxB];
+    int32_t wsum[32];
+  } hist;
+};
+
+// Exclusive scan of p[0..m) in place by the whole block (m up to millions).
+__device__ void block_exclusive_scan_inplace(int32_t *p, int64_t m, int32_t *wsum) {
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  const int64_t per = (m + kThreads - 1) / kThreads;
+  const int64_t lo = min64(m, t * per), hi = min64(m, lo + per);
+  uint32_t s = 0;
+  for (int64_t i = lo; i < hi; ++i) s += static_cast<uint32_t>(__ldcg(p + i));
+  uint32_t incl = s;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d) incl += y;
+  }
+  if (lane == 31) wsum[w] = static_cast<int32_t>(incl);
+  __syncthreads();
+  if (w == 0) {
+    const uint32_t x = lane < kWarps ? static_cast<uint32_t>(wsum[lane]) : 0u;
+    uint32_t xi = x;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, xi, d);
+      if (lane >= d) xi += y;
+    }
+    if (lane < kWarps) wsum[lane] = static_cast<int32_t>(xi - x);
+  }
+  __syncthreads();
+  uint32_t run = static_cast<uint32_t>(wsum[w]) + (incl - s);
+  for (int64_t i = lo; i < hi; ++i) {
+    const uint32_t v = static_cast<uint32_t>(__ldcg(p + i));
+    p[i] = static_cast<int32_t>(run);
+    run += v;
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(kThreads)
+    batch_kernel(const DevSeg *__restrict__ segs, const DevTask *__restrict__ tasks, int num_tasks,
+                 const int32_t *__restrict__ in0, const int32_t *__restrict__ in1,
+                 int32_t *__restrict__ out0, int32_t *__restrict__ out1, char *state,
+                 Ctrl *ctrl, unsigned long long *ticket, unsigned *abort_flag, bool tma,
+                 uint64_t timeout_ns, unsigned *fault) {
+  __shared__ BatchSmem sm;
+  __shared__ alignas(8) uint64_t bar;
+  __shared__ int s_task;
+  __shared__ int s_flag;
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  if (t == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  uint32_t phase = 0;
+  const unsigned lt = lanemask_lt_b();
+
+  while (true) {
+    if (t == 0) s_task = static_cast<int>(atomicAdd(ticket, 1ull));
+    __syncthreads();
+    const int task_id = s_task;
+    if (task_id >= num_tasks) break;
+    const DevTask task = tasks[task_id];
+    const DevSeg seg = segs[task.seg];
+    const int64_t tile_base = static_cast<int64_t>(task.tile) * kTile;
+    const int count = static_cast<int>(min64(kTile, seg.len - tile_base));
+    const int64_t gbase = seg.off + tile_base;
+
+    if (task.kind == kTaskScan) {
+      // ---- exclusive scan tile with look-back inside the segment ----
+      LookbackState<int32_t> st;
+      st.bind(state + seg.state, seg.tiles);
+      const bool tma_ok = tma && ((gbase & 3) == 0);  // 16-byte aligned tile start
+      const uint32_t bulk =
+          stage_tile<int32_t, kTile, kThreads>(sm.scan.tile, in0 + gbase, count, tma_ok, &bar);
+      if (bulk) {
+        if (!mbar_wait_bounded(&bar, phase, timeout_ns, fault)) atomicOr(abort_flag, 1u);
+        phase ^= 1u;
+      }
+      __syncthreads();
+      Chunk<int32_t> c[kChunks];
+      int32_t wex[kChunks];
+      TS32::phase1(sm.scan.tile, c, wex, sm.scan.sh);
+      __syncthreads();
+      if (w == 0) {
+        const int32_t agg = TS32::phase2_warp0(sm.scan.sh, lane);
+        int32_t prefix = 0;
+        bool ok = true;
+        if (task.tile == 0) {
+          if (lane == 0) st.publish(0, kFlagIncl, agg);
+        } else {
+          prefix = lookback_warp<int32_t>(st, task.tile, agg, lane, timeout_ns, fault, abort_flag,
+                                          ok);
+        }
+        if (lane == 0) sm.scan.sh.prefix = ok ? prefix : 0;
+      }
+      __syncthreads();
+      TS32::phase3<false>(c, wex, sm.scan.sh, sm.scan.sh.prefix);
+      TS32::store(out0, gbase, count, c, (reinterpret_cast<uintptr_t>(out0 + gbase) & 15) == 0);
+    } else if (task.kind == kTaskGather) {
+      // ---- permutation gather tile, indices local to the segment ----
+      const int32_t *src = in0 + seg.off;
+#pragma unroll
+      for (int k = 0; k < kTile / kThreads; k += 4) {
+        int v[4], idx[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int i = (k + q) * kThreads + t;
+          idx[q] = i < count ? in1[gbase + i] : -1;
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          v[q] = (idx[q] >= 0 && idx[q] < seg.len) ? __ldg(src + idx[q]) : 0;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int i = (k + q) * kThreads + t;
+          if (idx[q] >= 0 && idx[q] < seg.len) out0[gbase + i] = v[q];
+        }
+      }
+    } else if (task.kind == kTaskHist) {
+      // ---- bucket counts of a split tile ----
+      const unsigned mask = static_cast<unsigned>(seg.buckets - 1);
+      for (int b = t; b < seg.buckets; b += kThreads) sm.hist.cnt[b] = 0;
+      __syncthreads();
+      for (int i0 = 0; i0 < kTile; i0 += kThreads) {
+        const int i = i0 + t;
+        const bool valid = i < count;
+        const int b = valid ? static_cast<int>(static_cast<unsigned>(in0[gbase + i]) & mask) : -1;
+        const unsigned peers = __match_any_sync(0xffffffffu, b);
+        if (valid && (peers & lt) == 0u) atomicAdd(&sm.hist.cnt[b], static_cast<uint32_t>(__popc(peers)));
+      }
+      __syncthreads();
+      int32_t *his = reinterpret_cast<int32_t *>(state + seg.state);
+      for (int b = t; b < seg.buckets; b += kThreads)
+        his[static_cast<int64_t>(b) * seg.tiles + task.tile] = static_cast<int32_t>(sm.hist.cnt[b]);
+      __threadfence();
+      __syncthreads();
+      if (t == 0) {
+        const uint32_t prev = atomicAdd(&ctrl[task.seg].hist_done, 1u);
+        s_flag = (prev + 1 == static_cast<uint32_t>(seg.tiles)) ? 1 : 0;
+      }
+      __syncthreads();
+      if (s_flag) {  // last HIST tile of the segment: scan the histogram
+        __threadfence();
+        block_exclusive_scan_inplace(his, static_cast<int64_t>(seg.buckets) * seg.tiles,
+                                     sm.hist.wsum);
+        __threadfence();
+        __syncthreads();
+        if (t == 0) st_release_u32(&ctrl[task.seg].ready, 1u);
+      }
+    } else {
+      // ---- stable key/value scatter of a split tile ----
+      if (t == 0) {
+        bool ok = ld_acquire_u32(&ctrl[task.seg].ready) != 0u;
+        if (!ok) {
+          const uint64_t t0 = globaltimer_ns();
+          while (!(ok = ld_acquire_u32(&ctrl[task.seg].ready) != 0u)) {
+            if (globaltimer_ns() - t0 > timeout_ns || fault_raised(abort_flag)) break;
+            __nanosleep(100);
+          }
+        }
+        if (!ok) {
+          raise_fault(fault, EDPP_FAULT_TIMEOUT);
+          atomicOr(abort_flag, 1u);
+        }
+        s_flag = ok ? 1 : 0;
+      }
+      __syncthreads();
+      if (s_flag) {
+        const unsigned mask = static_cast<unsigned>(seg.buckets - 1);
+        const int B = seg.buckets;
+        const int32_t *his = reinterpret_cast<const int32_t *>(state + seg.state);
+        for (int i = t; i < count; i += kThreads) {
+          sm.split.keys[i] = in0[gbase + i];
+          sm.split.vals[i] = in1[gbase + i];
+        }
+        for (int i = t; i < kWarps * B; i += kThreads) sm.split.cnt16[i] = 0;
+        __syncthreads();
+        uint16_t *my = sm.split.cnt16 + w * B;
+        int32_t kk[kIters], vv[kIters];
+        uint32_t rk[kIters / 2];
+#pragma unroll
+        for (int it = 0; it < kIters; ++it) {
+          const int pos = w * kSeg + it * 32 + lane;
+          const bool valid = pos < count;
+          const int32_t key = valid ? sm.split.keys[pos] : 0;
+          const int32_t val = valid ? sm.split.vals[pos] : 0;
+          const int b = valid ? static_cast<int>(static_cast<unsigned>(key) & mask) : -1;
+          const unsigned peers = __match_any_sync(0xffffffffu, b);
+          const unsigned lower = peers & lt;
+          const uint16_t before = valid ? my[b] : 0;
+          __syncwarp();
+          if (valid && lower == 0u) my[b] = static_cast<uint16_t>(before + __popc(peers));
+          __syncwarp();
+          kk[it] = key;
+          vv[it] = val;
+          const uint32_t r = static_cast<uint32_t>(before + __popc(lower));
+          if (it & 1) rk[it >> 1] |= r << 16;
+          else rk[it >> 1] = r;
+        }
+        __syncthreads();
+        // per bucket: exclusive prefix over warps; tile counts; tile offsets
+        if (t < 32) {
+          int32_t run_total = 0;
+          for (int b0 = 0; b0 < B; b0 += 32) {
+            const int b = b0 + lane;
+            int32_t tot = 0;
+            if (b < B) {
+              for (int ww = 0; ww < kWarps; ++ww) {
+                const int32_t c = sm.split.cnt16[ww * B + b];
+                sm.split.cnt16[ww * B + b] = static_cast<uint16_t>(tot);
+                tot += c;
+              }
+            }
+            int32_t incl = tot;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+              const int32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+              if (lane >= d) incl += y;
+            }
+            if (b < B) {
+              const int32_t off = run_total + incl - tot;
+              sm.split.toff[b] = off;
+              sm.split.gofs[b] = __ldcg(his + static_cast<int64_t>(b) * seg.tiles + task.tile) - off;
+            }
+            run_total += __shfl_sync(0xffffffffu, incl, 31);
+          }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int it = 0; it < kIters; ++it) {
+          const int pos = w * kSeg + it * 32 + lane;
+          if (pos < count) {
+            const int b = static_cast<int>(static_cast<unsigned>(kk[it]) & mask);
+            const int r = static_cast<int>((rk[it >> 1] >> ((it & 1) * 16)) & 0xffffu);
+            const int s = sm.split.toff[b] + sm.split.cnt16[w * B + b] + r;
+            sm.split.keys[s] = kk[it];
+            sm.split.vals[s] = vv[it];
+          }
+        }
+        __syncthreads();
+        for (int s = t; s < count; s += kThreads) {
+          const int32_t key = sm.split.keys[s];
+          const int b = static_cast<int>(static_cast<unsigned>(key) & mask);
+          const int64_t o = seg.off + sm.split.gofs[b] + s;
+          out0[o] = key;
+          out1[o] = sm.split.vals[s];
+        }
+      }
+    }
+    __syncthreads();  // shared memory and s_task reused by the next task
+  }
+}
+
+}  // namespace
+
+// ---- host planner --------------------------------------------------------------
+namespace {
+
+constexpr size_t kHdrB = 256;  // ticket (u64) + abort flag (u32)
+
+int build_plan(const edpp_segment *in, int num, const edpp_batch_tuning *tune, BatchPlanImpl &p) {
+  p.num_segs = num;
+  p.segs.resize(static_cast<size_t>(num));
+  std::vector<int> order(static_cast<size_t>(num));
+  std::iota(order.begin(), order.end(), 0);
+  const int defer = tune ? std::max(0, tune->split_defer_segments) : 1;
+  const bool largest_first = tune ? tune->largest_first != 0 : true;
+  p.blocks_per_sm = tune && tune->blocks_per_sm > 0 ? tune->blocks_per_sm : 4;
+  if (largest_first)
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return in[a].length > in[b].length; });
+  // state: scan tile words first (zeroed per launch), then split histograms
+  size_t scan_state = 0, split_state = 0;
+  for (int i = 0; i < num; ++i) {
+    const edpp_segment &s = in[i];
+    if (s.length < 0 || s.offset < 0) return EDPP_EINVAL;
+    if (s.op != EDPP_BATCH_SCAN && s.op != EDPP_BATCH_SPLIT && s.op != EDPP_BATCH_GATHER)
+      return EDPP_EINVAL;
+    if (s.op == EDPP_BATCH_SPLIT &&
+        (s.buckets < 1 || s.buckets > kMaxB || (s.buckets & (s.buckets - 1))))
+      return EDPP_EINVAL;
+    DevSeg d{};
+    d.off = s.offset;
+    d.len = s.length;
+    d.op = s.op;
+    d.tiles = static_cast<int32_t>((static_cast<int64_t>(s.length) + kTile - 1) / kTile);
+    d.buckets = s.op == EDPP_BATCH_SPLIT ? s.buckets : 0;
+    if (s.op == EDPP_BATCH_SCAN) {
+      d.state = static_cast<int64_t>(scan_state);
+      scan_state += LookbackState<int32_t>::bytes(d.tiles);
+    }
+    p.segs[static_cast<size_t>(i)] = d;
+    p.total_elems += s.length;
+  }
+  for (int i = 0; i < num; ++i) {
+    DevSeg &d = p.segs[static_cast<size_t>(i)];
+    if (d.op == EDPP_BATCH_SPLIT) {
+      d.state = static_cast<int64_t>(scan_state + split_state);
+      split_state += round_up(static_cast<size_t>(d.buckets) * d.tiles * 4, 256);
+    }
+  }
+  p.scan_state_bytes = scan_state;
+  p.state_bytes = scan_state + split_state;
+  // task queue: segments in order; a split's SPLIT tasks follow `defer`
+  // segments after its HIST tasks (so the histogram scan overlaps other work)
+  std::vector<std::vector<DevTask>> pending;  // deferred split scatter lists
+  std::vector<int> pending_age;
+  auto flush_due = [&](bool all) {
+    for (size_t k = 0; k < pending.size();) {
+      if (all || pending_age[k] >= defer) {
+        p.tasks.insert(p.tasks.end(), pending[k].begin(), pending[k].end());
+        pending.erase(pending.begin() + static_cast<long>(k));
+        pending_age.erase(pending_age.begin() + static_cast<long>(k));
+      } else {
+        ++k;
+      }
+    }
+  };
+  for (int oi = 0; oi < num; ++oi) {
+    const int i = order[static_cast<size_t>(oi)];
+    const DevSeg &d = p.segs[static_cast<size_t>(i)];
+    for (auto &a : pending_age) ++a;
+    flush_due(false);
+    if (d.len == 0) continue;
+    if (d.op == EDPP_BATCH_SCAN) {
+      for (int t = 0; t < d.tiles; ++t) p.tasks.push_back({i, t, kTaskScan, 0});
+    } else if (d.op == EDPP_BATCH_GATHER) {
+      for (int t = 0; t < d.tiles; ++t) p.tasks.push_back({i, t, kTaskGather, 0});
+    } else {
+      for (int t = 0; t < d.tiles; ++t) p.tasks.push_back({i, t, kTaskHist, 0});
+      std::vector<DevTask> sc;
+      for (int t = 0; t < d.tiles; ++t) sc.push_back({i, t, kTaskSplit, 0});
+      pending.push_back(std::move(sc));
+      pending_age.push_back(0);
+    }
+  }
+  flush_due(true);
+  size_t o = kHdrB;
+  p.off_segs = o;
+  o += round_up(sizeof(DevSeg) * p.segs.size(), 256);
+  p.off_tasks = o;
+  o += round_up(sizeof(DevTask) * p.tasks.size(), 256);
+  p.off_ctrl = o;
+  o += round_up(sizeof(Ctrl) * p.segs.size(), 256);
+  p.off_state = o;
+  o += round_up(p.state_bytes, 256);
+  p.bytes = o;
+  return EDPP_OK;
+}
+
+}  // namespace
+}  // namespace edpp
+
+using edpp::BatchPlanImpl;
+
+extern "C" {
+
+int edpp_batch_plan_create(const edpp_segment *segs, int num_segs, const edpp_batch_tuning *tuning,
+                           edpp_batch_plan **out) {
+  if (!out || num_segs < 0 || (num_segs > 0 && !segs)) return EDPP_EINVAL;
+  auto *p = new (std::nothrow) edpp_batch_plan;
+  if (!p) return EDPP_ENOMEM;
+  const int s = edpp::build_plan(segs, num_segs, tuning, p->impl);
+  if (s != EDPP_OK) {
+    delete p;
+    return s;
+  }
+  *out = p;
+  return EDPP_OK;
+}
+
+void edpp_batch_plan_destroy(edpp_batch_plan *plan) { delete plan; }
+
+size_t edpp_batch_plan_workspace_size(const edpp_batch_plan *plan) {
+  return plan ? plan->impl.bytes : 0;
+}
+
+int edpp_batch_plan_num_tasks(const edpp_batch_plan *plan) {
+  return plan ? static_cast<int>(plan->impl.tasks.size()) : 0;
+}
+
+int edpp_batch_plan_upload(const edpp_batch_plan *plan, void *ws, size_t ws_bytes, void *stream) {
+  if (!plan || !ws) return EDPP_EINVAL;
+  const BatchPlanImpl &p = plan->impl;
+  if (ws_bytes < p.bytes) return EDPP_ENOMEM;
+  cudaStream_t st = edpp::as_stream(stream);
+  char *w = static_cast<char *>(ws);
+  if (!p.segs.empty() &&
+      cudaMemcpyAsync(w + p.off_segs, p.segs.data(), sizeof(edpp::DevSeg) * p.segs.size(),
+                      cudaMemcpyHostToDevice, st) != cudaSuccess)
+    return EDPP_ECUDA;
+  if (!p.tasks.empty() &&
+      cudaMemcpyAsync(w + p.off_tasks, p.tasks.data(), sizeof(edpp::DevTask) * p.tasks.size(),
+                      cudaMemcpyHostToDevice, st) != cudaSuccess)
+    return EDPP_ECUDA;
+  // pageable sources: make the copies complete before the plan can change
+  return edpp::cuda_status(cudaStreamSynchronize(st));
+}
+
+int edpp_batch_launch(const edpp_batch_plan *plan, const int32_t *in0, const int32_t *in1,
+                      int32_t *out0, int32_t *out1, void *ws, size_t ws_bytes, void *stream) {
+  using namespace edpp;
+  if (!plan || !ws) return EDPP_EINVAL;
+  const BatchPlanImpl &p = plan->impl;
+  if (ws_bytes < p.bytes) return EDPP_ENOMEM;
+  if (p.tasks.empty()) return EDPP_OK;
+  if (!in0 || !out0) return EDPP_EINVAL;
+  unsigned *fault = fault_word();
+  if (!fault) return EDPP_ECUDA;
+  cudaStream_t st = as_stream(stream);
+  char *w = static_cast<char *>(ws);
+  // zero: ticket + abort flag, per-segment control words, scan tile states
+  if (cudaMemsetAsync(w, 0, kHdrB, st) != cudaSuccess) return EDPP_ECUDA;
+  if (cudaMemsetAsync(w + p.off_ctrl, 0, p.off_state - p.off_ctrl + p.scan_state_bytes, st) !=
+      cudaSuccess)
+    return EDPP_ECUDA;
+  const int sms = device_sm_count();
+  int64_t blocks = static_cast<int64_t>(sms) * p.blocks_per_sm;
+  blocks = min64(blocks, static_cast<int64_t>(p.tasks.size()));
+  batch_kernel<<<static_cast<unsigned>(max64(blocks, 1)), kThreads, 0, st>>>(
+      reinterpret_cast<const DevSeg *>(w + p.off_segs),
+      reinterpret_cast<const DevTask *>(w + p.off_tasks), static_cast<int>(p.tasks.size()), in0,
+      in1, out0, out1, w + p.off_state, reinterpret_cast<Ctrl *>(w + p.off_ctrl),
+      reinterpret_cast<unsigned long long *>(w), reinterpret_cast<unsigned *>(w + 8),
+      aligned16(in0), kDefaultWaitNs, fault);
+  return launch_status();
+}
+
+}  // extern "C"
+
+// ---- plain per-array launches (the baseline the batch replaces) ---------------
+extern "C" size_t edpp_batch_plain_workspace_size(const edpp_segment *segs, int num_segs) {
+  size_t m = 0;
+  for (int i = 0; i < num_segs; ++i) {
+    const edpp_segment &s = segs[i];
+    size_t b = 0;
+    if (s.op == EDPP_BATCH_SCAN) b = edpp_scan_workspace_size(s.length, EDPP_I32, EDPP_SCAN_LOOKBACK);
+    else if (s.op == EDPP_BATCH_SPLIT) b = edpp_split_workspace_size(s.length, s.buckets, EDPP_KVS_SOA);
+    m = std::max(m, b);
+  }
+  return m;
+}
+
+// One C-ABI call per segment, issued back to back on `stream` from this host
+// loop; one workspace serves every call (calls are ordered on the stream).
+// Gather segments use segment-local indices, so they run as one-pass gathers
+// of the segment's slice.
+extern "C" int edpp_batch_run_plain(const edpp_segment *segs, int num_segs, const int32_t *in0,
+                                    const int32_t *in1, int32_t *out0, int32_t *out1, void *ws,
+                                    size_t ws_bytes, void *stream) {
+  for (int i = 0; i < num_segs; ++i) {
+    const edpp_segment &s = segs[i];
+    if (s.length == 0) continue;
+    int st;
+    if (s.op == EDPP_BATCH_SCAN)
+      st = edpp_scan_exclusive_i32(in0 + s.offset, out0 + s.offset, s.length, EDPP_SCAN_LOOKBACK,
+                                   ws, ws_bytes, stream);
+    else if (s.op == EDPP_BATCH_SPLIT)
+      st = edpp_split_i32(in0 + s.offset, out0 + s.offset, nullptr, s.length, s.buckets,
+                          EDPP_KVS_SOA, in1 + s.offset, out1 + s.offset, ws, ws_bytes, stream);
+    else if (s.op == EDPP_BATCH_GATHER)
+      st = edpp_gather_i32(in0 + s.offset, out0 + s.offset, s.length, in1 + s.offset, 1, stream);
+    else
+      st = EDPP_EINVAL;
+    if (st != EDPP_OK) return st;
+  }
+  return EDPP_OK;
+}
+
+// ---- autotuner ----------------------------------------------------------------------
+// Times every candidate schedule on this GPU for the given segments (CUDA
+// events around `reps` launches after one warm-up) and returns the fastest.
+// Candidates: blocks per SM {2,3,4,6,8} x split deferral {0,1,2,4} x
+// segment order {given, largest first}.  The workspace must fit the plan
+// (edpp_batch_plan_workspace_size; it does not depend on the tuning).
+extern "C" int edpp_batch_autotune(const edpp_segment *segs, int num_segs, const int32_t *in0,
+                                   const int32_t *in1, int32_t *out0, int32_t *out1, void *ws,
+                                   size_t ws_bytes, void *stream, int reps,
+                                   edpp_batch_tuning *best, float *best_ms) {
+  if (!best || reps < 1) return EDPP_EINVAL;
+  cudaStream_t st = edpp::as_stream(stream);
+  cudaEvent_t a, b;
+  if (cudaEventCreate(&a) != cudaSuccess) return EDPP_ECUDA;
+  if (cudaEventCreate(&b) != cudaSuccess) {
+    cudaEventDestroy(a);
+    return EDPP_ECUDA;
+  }
+  float best_t = 1e30f;
+  int status = EDPP_OK;
+  for (int bps : {2, 3, 4, 6, 8}) {
+    for (int defer : {0, 1, 2, 4}) {
+      for (int lf : {0, 1}) {
+        edpp_batch_tuning tu{bps, defer, lf, 0};
+        edpp_batch_plan *plan = nullptr;
+        status = edpp_batch_plan_create(segs, num_segs, &tu, &plan);
+        if (status != EDPP_OK) break;
+        status = edpp_batch_plan_upload(plan, ws, ws_bytes, stream);
+        if (status == EDPP_OK)
+          status = edpp_batch_launch(plan, in0, in1, out0, out1, ws, ws_bytes, stream);
+        if (status == EDPP_OK && cudaEventRecord(a, st) != cudaSuccess) status = EDPP_ECUDA;
+        for (int r = 0; r < reps && status == EDPP_OK; ++r)
+          status = edpp_batch_launch(plan, in0, in1, out0, out1, ws, ws_bytes, stream);
+        if (status == EDPP_OK && cudaEventRecord(b, st) != cudaSuccess) status = EDPP_ECUDA;
+        if (status == EDPP_OK) status = edpp_sync_status(stream, 0);
+        float ms = 0;
+        if (status == EDPP_OK && cudaEventElapsedTime(&ms, a, b) != cudaSuccess) status = EDPP_ECUDA;
+        edpp_batch_plan_destroy(plan);
+        if (status != EDPP_OK) break;
+        ms /= reps;
+        if (ms < best_t) {
+          best_t = ms;
+          *best = tu;
+        }
+      }
+      if (status != EDPP_OK) break;
+    }
+    if (status != EDPP_OK) break;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (best_ms) *best_ms = best_t;
+  return status;
+}

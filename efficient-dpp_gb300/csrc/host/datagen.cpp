@@ -12,6 +12,7 @@
 // openmp/util/utility.cpp:77-85; random_generator_int_unique seeds from
 // time(), :90-104), so these replace them.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdint>
 #include <thread>
@@ -119,6 +120,55 @@ void edpp_gen_permutation_i32(int32_t *out, int64_t n, uint64_t seed) {
                                                    static_cast<uint64_t>(i + 1)));
     std::swap(out[i], out[j]);
   }
+}
+
+// Inputs of a batch of segments (same layout as edpp_segment: offset,
+// length, op, buckets, reserved), filled in parallel over segments; segment i
+// uses seeds derived from (seed, i):
+//   op 0 (scan):   in0 uniform in [0,100]
+//   op 1 (split):  in0 keys uniform over [0,2^31), in1 = local index
+//   op 2 (gather): in0 uniform int32, in1 a Fisher-Yates permutation of
+//                  [0, length)
+void edpp_gen_batch_inputs(const void *segs_v, int num_segs, uint64_t seed, int32_t *in0,
+                           int32_t *in1) {
+  struct Seg {
+    int64_t offset;
+    int32_t length, op, buckets, reserved;
+  };
+  const Seg *segs = static_cast<const Seg *>(segs_v);
+  unsigned nt = std::thread::hardware_concurrency();
+  if (nt == 0) nt = 1;
+  if (nt > 64) nt = 64;
+  std::atomic<int> next{0};
+  std::vector<std::thread> ts;
+  for (unsigned t = 0; t < nt; ++t) {
+    ts.emplace_back([&] {
+      for (int i = next++; i < num_segs; i = next++) {
+        const Seg &s = segs[i];
+        const uint64_t sd = mix64(seed * 0x100000001B3ull + static_cast<uint64_t>(i));
+        int32_t *a = in0 + s.offset;
+        int32_t *b = in1 + s.offset;
+        const int64_t n = s.length;
+        if (s.op == 0) {
+          for (int64_t k = 0; k < n; ++k) a[k] = static_cast<int32_t>(bounded(draw(sd, k), 101));
+          for (int64_t k = 0; k < n; ++k) b[k] = 0;
+        } else if (s.op == 1) {
+          for (int64_t k = 0; k < n; ++k) a[k] = static_cast<int32_t>(draw(sd, k) >> 33);
+          for (int64_t k = 0; k < n; ++k) b[k] = static_cast<int32_t>(k);
+        } else {
+          for (int64_t k = 0; k < n; ++k) a[k] = static_cast<int32_t>(draw(sd, k) >> 32);
+          for (int64_t k = 0; k < n; ++k) b[k] = static_cast<int32_t>(k);
+          const uint64_t sp = sd ^ 0x2545F4914F6CDD1Dull;
+          for (int64_t k = n - 1; k > 0; --k) {
+            const int64_t j = static_cast<int64_t>(
+                bounded(draw(sp, static_cast<uint64_t>(n - 1 - k)), static_cast<uint64_t>(k + 1)));
+            std::swap(b[k], b[j]);
+          }
+        }
+      }
+    });
+  }
+  for (auto &t : ts) t.join();
 }
 
 }  // extern "C"

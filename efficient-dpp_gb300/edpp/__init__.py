@@ -66,6 +66,24 @@ SIGNATURES = {
     "edpp_selftest_lookback_timeout": (_I, [_VP, _VP, _I64, _U64, _VP, _SZ, _VP]),
     "edpp_scan_exclusive_i32_noalloc": (_I, [_VP, _VP, _I64, _VP]),
     "edpp_scan_exclusive_i32_noalloc_max_length": (_I64, []),
+    # batched segments
+    "edpp_batch_plan_create": (_I, [_VP, _I, _VP, ctypes.POINTER(_VP)]),
+    "edpp_batch_plan_destroy": (None, [_VP]),
+    "edpp_batch_plan_workspace_size": (_SZ, [_VP]),
+    "edpp_batch_plan_num_tasks": (_I, [_VP]),
+    "edpp_batch_plan_upload": (_I, [_VP, _VP, _SZ, _VP]),
+    "edpp_batch_launch": (_I, [_VP, _VP, _VP, _VP, _VP, _VP, _SZ, _VP]),
+    "edpp_batch_autotune": (_I, [_VP, _I, _VP, _VP, _VP, _VP, _VP, _SZ, _VP, _I, _VP,
+                                 ctypes.POINTER(ctypes.c_float)]),
+    "edpp_batch_plain_workspace_size": (_SZ, [_VP, _I]),
+    "edpp_batch_run_plain": (_I, [_VP, _I, _VP, _VP, _VP, _VP, _VP, _SZ, _VP]),
+    "edpp_gen_batch_inputs": (None, [_VP, _I, _U64, _VP, _VP]),
+    # serving (edpp.serve binds these with structure types)
+    "edpp_server_create": (_I, [_VP, _VP]),
+    "edpp_server_submit": (_I, [_VP, _VP, _VP]),
+    "edpp_server_wait": (_I, [_VP, _U64, ctypes.c_double, _VP]),
+    "edpp_server_get_stats": (_I, [_VP, _VP]),
+    "edpp_server_destroy": (None, [_VP]),
     # host generators
     "edpp_gen_draw": (_U64, [_U64, _U64]),
     "edpp_gen_uniform_i32": (None, [_VP, _I64, _U64, _I64, _I64]),

@@ -227,6 +227,126 @@ int edpp_scan_exclusive_i32_noalloc(const int32_t *in, int32_t *out, int64_t len
                                     void *stream);
 int64_t edpp_scan_exclusive_i32_noalloc_max_length(void);
 
+/* ---- batched segments (one persistent launch) --------------------------- */
+
+/* Operations a batch segment can run.  Results equal the plain calls:
+ *   SCAN    out0 = exclusive int32 scan of in0            (edpp_scan_exclusive_i32)
+ *   SPLIT   (out0, out1) = stable split of keys in0 / values in1 by
+ *           key & (buckets-1), buckets a power of two <= 256  (edpp_split_i32, SOA)
+ *   GATHER  out0[i] = in0[off + in1[i]] with segment-local indices in1
+ *           (entries outside [0, length) skipped)       (edpp_gather_i32)
+ * No reference counterpart: the reference runs one primitive per call. */
+typedef enum {
+    EDPP_BATCH_SCAN = 0,
+    EDPP_BATCH_SPLIT = 1,
+    EDPP_BATCH_GATHER = 2
+} edpp_batch_op;
+
+/* One segment: elements [offset, offset+length) of the batch arrays. */
+typedef struct {
+    int64_t offset;
+    int32_t length;
+    int32_t op;       /* edpp_batch_op */
+    int32_t buckets;  /* SPLIT only */
+    int32_t reserved;
+} edpp_segment;
+
+/* Scheduling knobs (chosen per size class by the project's autotuner,
+ * edpp_batch_autotune).  Zero-initialised = defaults. */
+typedef struct {
+    int32_t blocks_per_sm;         /* persistent grid: blocks per SM (default 4)  */
+    int32_t split_defer_segments;  /* SPLIT tiles queued this many segments after
+                                      their HIST tiles (default 1)               */
+    int32_t largest_first;         /* 1: queue segments by descending length      */
+    int32_t reserved;
+} edpp_batch_tuning;
+
+typedef struct edpp_batch_plan edpp_batch_plan;  /* opaque, host side */
+
+/* Build the task queue for `num_segs` segments (host only, no GPU work). */
+int edpp_batch_plan_create(const edpp_segment *segs, int num_segs,
+                           const edpp_batch_tuning *tuning, edpp_batch_plan **plan);
+void edpp_batch_plan_destroy(edpp_batch_plan *plan);
+size_t edpp_batch_plan_workspace_size(const edpp_batch_plan *plan);
+int edpp_batch_plan_num_tasks(const edpp_batch_plan *plan);
+/* Copy the plan's tables into the workspace (synchronises `stream`). */
+int edpp_batch_plan_upload(const edpp_batch_plan *plan, void *ws, size_t ws_bytes,
+                           void *stream);
+/* Run every segment in one persistent launch (plus two memsets).  The
+ * workspace must hold an uploaded plan.  Stream-ordered; may be captured in a
+ * CUDA graph and replayed while the plan and arrays stay the same. */
+int edpp_batch_launch(const edpp_batch_plan *plan, const int32_t *in0,
+                      const int32_t *in1, int32_t *out0, int32_t *out1, void *ws,
+                      size_t ws_bytes, void *stream);
+
+/* Autotuner: times every candidate edpp_batch_tuning on this GPU for these
+ * segments and writes the fastest to *best (its mean ms to *best_ms).
+ * Synchronises `stream`; overwrites out0/out1. */
+int edpp_batch_autotune(const edpp_segment *segs, int num_segs, const int32_t *in0,
+                        const int32_t *in1, int32_t *out0, int32_t *out1, void *ws,
+                        size_t ws_bytes, void *stream, int reps, edpp_batch_tuning *best,
+                        float *best_ms);
+
+/* The same segments as one plain C-ABI call each, back to back on `stream`
+ * (the per-array baseline of the batch).  Workspace: the largest any one
+ * call needs. */
+size_t edpp_batch_plain_workspace_size(const edpp_segment *segs, int num_segs);
+int edpp_batch_run_plain(const edpp_segment *segs, int num_segs, const int32_t *in0,
+                         const int32_t *in1, int32_t *out0, int32_t *out1, void *ws,
+                         size_t ws_bytes, void *stream);
+
+/* ---- serving: continuous batching of requests --------------------------- */
+
+/* A request: one scan / split / gather (edpp_batch_op) on HOST arrays of
+ * `length` int32 (pinned memory gives asynchronous copies).  in1: split
+ * values or segment-local gather indices; out1: split values. */
+typedef struct {
+    int32_t op;
+    int32_t buckets;
+    int64_t length;
+    const int32_t *in0;
+    const int32_t *in1;
+    int32_t *out0;
+    int32_t *out1;
+} edpp_request;
+
+typedef struct {
+    size_t pool_bytes;           /* device memory for request buffers (admission cap) */
+    int32_t slots;               /* batches in flight at once (streams), 1..16         */
+    int32_t max_batch_requests;  /* per batch (default 1024)                          */
+    int64_t max_batch_elements;  /* per batch (default: the whole pool)               */
+    edpp_batch_tuning tuning;    /* schedule of the batch kernel                      */
+} edpp_server_config;
+
+typedef struct {
+    double queue_ms;    /* submit -> admitted into a batch                     */
+    double latency_ms;  /* submit -> outputs back in host memory               */
+} edpp_request_timing;
+
+typedef struct {
+    int64_t submitted, completed, batches, elements_done;
+    int64_t max_requests_per_batch, max_pool_bytes_used, max_batches_in_flight;
+} edpp_server_stats;
+
+typedef struct edpp_server edpp_server;  /* opaque */
+
+/* Start a server on the current device: allocates the request pool (four
+ * arenas of pool_bytes/4), per-slot streams and workspaces, and a scheduler
+ * thread.  One scheduler loop retires finished batches, admits waiting
+ * requests in arrival order while pool memory and a slot are free, and
+ * launches each batch as one persistent kernel between its copies.  No
+ * reference counterpart. */
+int edpp_server_create(const edpp_server_config *cfg, edpp_server **server);
+/* Thread-safe, non-blocking.  EDPP_EINVAL for a malformed request or one
+ * larger than the whole pool. */
+int edpp_server_submit(edpp_server *server, const edpp_request *req, uint64_t *id);
+/* Block until request `id` completes (outputs written); returns its status. */
+int edpp_server_wait(edpp_server *server, uint64_t id, double timeout_s,
+                     edpp_request_timing *timing);
+int edpp_server_get_stats(edpp_server *server, edpp_server_stats *stats);
+/* Finish all submitted work, stop the scheduler, free everything. */
+void edpp_server_destroy(edpp_server *server);
+
 /* ---- bounded-wait self-test --------------------------------------------- */
 
 /* Runs a look-back scan over `length` int32 elements whose first tile is

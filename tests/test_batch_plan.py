@@ -1,0 +1,62 @@
+"""Host side of the batched form: the config-5 segment table, the planner,
+and its argument checks (no GPU)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+
+@pytest.fixture(scope="module")
+def batch(edpp):
+    from edpp import batch as b
+    return b
+
+
+def test_config5_segments(batch):
+    segs = batch.config5_segments()
+    assert len(segs) == 4096
+    L = segs["length"].astype(np.int64)
+    assert L.min() >= 1024 and L.sum() <= 1 << 30
+    assert L.sum() > 0.99 * (1 << 30) - 4096 * 1024  # the cap is used
+    assert set(np.unique(segs["op"])) == {0, 1, 2}
+    assert np.all(segs["offset"] % 64 == 0)
+    assert np.all(np.diff(segs["offset"]) >= L[:-1])  # no overlap
+    assert np.all(segs["buckets"][segs["op"] == 1] == 64)
+    # log-uniform before scaling: sizes span ~ 4 decades
+    assert L.max() / L.min() > 1000
+    np.testing.assert_array_equal(segs, batch.config5_segments())  # deterministic
+
+
+def test_plan_tasks_and_workspace(batch):
+    segs = batch.layout([1, 4096, 4097, 100000, 0, 5000], [0, 1, 2, 1, 0, 2])
+    plan = batch.Plan(segs)
+    tiles = [1, 1, 2, 25, 0, 2]
+    # split segments have a HIST and a SPLIT task per tile
+    expect = sum(t * (2 if op == 1 else 1) for t, op in zip(tiles, [0, 1, 2, 1, 0, 2]))
+    assert plan.num_tasks == expect
+    assert plan.workspace_bytes > 0
+    for tu in (batch.Tuning(2, 0, 0, 0), batch.Tuning(8, 4, 1, 0)):
+        p2 = batch.Plan(segs, tu)
+        assert p2.num_tasks == expect and p2.workspace_bytes == plan.workspace_bytes
+
+
+def test_plan_rejects_bad_segments(batch, edpp):
+    lib = edpp.lib()
+    for bad in ([(0, 10, 7, 0, 0)], [(0, 10, 1, 3, 0)], [(0, 10, 1, 512, 0)], [(0, -1, 0, 0, 0)]):
+        segs = np.array(bad, batch.SEG_DTYPE)
+        h = ctypes.c_void_p()
+        assert lib.edpp_batch_plan_create(ctypes.c_void_p(segs.ctypes.data), 1, None,
+                                          ctypes.byref(h)) == edpp.EDPP_EINVAL
+
+
+def test_inputs_deterministic(batch):
+    segs = batch.layout([3000, 5000, 7000], [0, 1, 2])
+    a0, a1 = batch.gen_inputs(segs, seed=4)
+    b0, b1 = batch.gen_inputs(segs, seed=4)
+    np.testing.assert_array_equal(a0, b0)
+    np.testing.assert_array_equal(a1, b1)
+    g = segs[2]
+    idx = a1[g["offset"]:g["offset"] + g["length"]]
+    assert np.array_equal(np.sort(idx), np.arange(g["length"], dtype=np.int32))
+    sc = a0[:3000]
+    assert sc.min() >= 0 and sc.max() <= 100
