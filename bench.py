@@ -453,6 +453,138 @@ def run_serve_workload(args, rank, world):
     return 0
 
 
+def _event_ms(fn, reps, warmup, flush=None):
+    """Mean CUDA-event time of fn() over reps calls (after warm-up); with
+    `flush`, an L2-sized buffer is rewritten before every call and the flush
+    is timed separately and subtracted."""
+    import torch
+    stream = torch.cuda.current_stream()
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    total = 0.0
+    for _ in range(reps):
+        if flush is not None:
+            flush.add_(1)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        total += e0.elapsed_time(e1)
+    return total / reps
+
+
+def run_scan_workload(args, rank, world):
+    """Configs 1 and 4: int32 exclusive scan of 2^24 values in [0,15]
+    (seed 1), warm and with L2 flushed; global scans of 2^30 int32 / int64
+    (inclusive and exclusive, values in [0,100], seed 1) and f32 inclusive
+    (values in [-1,1], seed 1) under the three schemes."""
+    import numpy as np
+    import torch
+
+    import edpp
+    edpp.lib()
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.set_device(dev)
+    peak, peak_kind = measured_peak_gbs()
+    rows = []
+    flush = torch.empty(64 << 20, dtype=torch.int32, device=dev)  # 256 MB > L2
+    x24 = torch.from_numpy(edpp.gen_uniform_i32(1 << 24, 1, 0, 15)).to(dev)
+    y24 = torch.empty_like(x24)
+    for algo in ("lookback", "rts", "ssa"):
+        ws = edpp.workspace(edpp.scan_workspace_bytes(1 << 24, "int32", algo), dev)
+        for l2 in ("warm", "flushed"):
+            ms = _event_ms(lambda: edpp.scan(x24, algo=algo, out=y24, ws=ws), args.steps,
+                           args.warmup, flush if l2 == "flushed" else None)
+            gbs = 8 * (1 << 24) / (ms * 1e-3) / 1e9
+            rows.append({"config": "1", "n": 1 << 24, "dtype": "int32", "inclusive": False,
+                         "algo": algo, "l2": l2, "ms": round(ms, 4), "GB/s": round(gbs, 1),
+                         "frac_of_hbm": round(gbs / peak, 4)})
+    del x24, y24
+    n = 1 << args.scan_log2n
+    for dt, bpe in (("int32", 8), ("int64", 16), ("float32", 8)):
+        if dt == "int32":
+            x = torch.from_numpy(edpp.gen_uniform_i32(n, 1, 0, 100)).to(dev)
+        elif dt == "int64":
+            x = torch.from_numpy(edpp.gen_uniform_i64(n, 1, 0, 100)).to(dev)
+        else:
+            x = torch.from_numpy(edpp.gen_uniform_f32(n, 1, -1.0, 1.0)).to(dev)
+        y = torch.empty_like(x)
+        for inc in ((False, True) if dt != "float32" else (True,)):
+            for algo in ("lookback", "rts", "ssa"):
+                ws = edpp.workspace(edpp.scan_workspace_bytes(n, dt, algo), dev)
+                ms = _event_ms(lambda: edpp.scan(x, inclusive=inc, algo=algo, out=y, ws=ws),
+                               args.steps, args.warmup)
+                gbs = bpe * n / (ms * 1e-3) / 1e9
+                rows.append({"config": "4", "n": n, "dtype": dt, "inclusive": inc, "algo": algo,
+                             "ms": round(ms, 4), "GB/s": round(gbs, 1),
+                             "frac_of_hbm": round(gbs / peak, 4)})
+                del ws
+        del x, y
+        torch.cuda.empty_cache()
+    if edpp.sync_status() != edpp.EDPP_OK:
+        raise SystemExit("device fault in the scan workload")
+    head = [r for r in rows if r["config"] == "1" and r["algo"] == "lookback" and r["l2"] == "flushed"][0]
+    if rank == 0:
+        print(json.dumps({"metric": METRIC, "workload_metric": "scan GB/s (8 B/elem int32)",
+                          "value": head["GB/s"], "unit": "GB/s", "n_gpus": world,
+                          "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["ms"],
+                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                          "dtype": "int32", "data": "synthetic", "peak": peak,
+                          "peak_source": peak_kind,
+                          "config": {"workload": "scans: config 1 (2^24 int32 [0,15] seed 1) "
+                                                 "and config 4 (2^30, three schemes)"},
+                          "rows": rows}), flush=True)
+    return 0
+
+
+def run_split_workload(args, rank, world):
+    """Config 3: stable split of 2^28 (int32 key, int32 value = index) pairs,
+    B = 2..1024, keys uniform over [0,2^31) or Zipf(1.0) buckets (seed 3)."""
+    import numpy as np
+    import torch
+
+    import edpp
+    edpp.lib()
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.set_device(dev)
+    peak, peak_kind = measured_peak_gbs()
+    n = 1 << args.split_log2n
+    vals = torch.arange(n, dtype=torch.int32, device=dev)
+    ko = torch.empty(n, dtype=torch.int32, device=dev)
+    vo = torch.empty_like(ko)
+    ws = edpp.workspace(edpp.split_workspace_bytes(n, 4096, "soa"), dev)
+    uniform = torch.from_numpy(edpp.gen_keys_uniform(n, 3)).to(dev)
+    rows = []
+    for B in [2 ** k for k in range(1, 11)]:
+        for kind in ("uniform", "zipf"):
+            keys = uniform if kind == "uniform" else \
+                torch.from_numpy(edpp.gen_keys_zipf(n, 3, B, 1.0)).to(dev)
+            ms = _event_ms(lambda: edpp.split(keys, B, values=vals, keys_out=ko, values_out=vo,
+                                              ws=ws), args.steps, args.warmup)
+            gbs = 16 * n / (ms * 1e-3) / 1e9
+            rows.append({"buckets": B, "keys": kind, "ms": round(ms, 4), "GB/s": round(gbs, 1),
+                         "frac_of_hbm": round(gbs / peak, 4)})
+            if kind == "zipf":
+                del keys
+    if edpp.sync_status() != edpp.EDPP_OK:
+        raise SystemExit("device fault in the split workload")
+    head = [r for r in rows if r["buckets"] == 256 and r["keys"] == "uniform"][0]
+    if rank == 0:
+        print(json.dumps({"metric": METRIC, "workload_metric": "stable split GB/s (16 B/pair)",
+                          "value": head["GB/s"], "unit": "GB/s", "n_gpus": world,
+                          "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["ms"],
+                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                          "dtype": "int32", "data": "synthetic", "peak": peak,
+                          "peak_source": peak_kind,
+                          "config": {"workload": f"split 2^{args.split_log2n} KV, B=2..1024, "
+                                                 "uniform / Zipf(1.0) keys, seed 3"},
+                          "rows": rows}), flush=True)
+    return 0
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawTextHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -468,7 +600,8 @@ def main(argv=None):
                     help="gather/scatter schedule of the timed step")
     ap.add_argument("--no-compare", action="store_true",
                     help="skip timing the other gather/scatter schedule")
-    ap.add_argument("--workload", default="gs_stream", choices=["gs_stream", "batch", "serve"],
+    ap.add_argument("--workload", default="gs_stream",
+                    choices=["gs_stream", "batch", "serve", "scan", "split"],
                     help="gs_stream: multi-pass gather/scatter + STREAM (default); "
                          "batch: 4096 uneven segments, batched vs plain; "
                          "serve: Poisson request stream through the server")
@@ -477,6 +610,8 @@ def main(argv=None):
     ap.add_argument("--serve-payloads", type=int, default=48)
     ap.add_argument("--serve-slots", type=int, default=4)
     ap.add_argument("--pool-gb", type=float, default=40.0)
+    ap.add_argument("--scan-log2n", type=int, default=30)
+    ap.add_argument("--split-log2n", type=int, default=28)
     ap.add_argument("--autotune", action="store_true",
                     help="batch: run the autotuner and record its choice")
     args = ap.parse_args(argv)
@@ -489,6 +624,10 @@ def main(argv=None):
         return run_batch_workload(args, rank, world)
     if args.workload == "serve":
         return run_serve_workload(args, rank, world)
+    if args.workload == "scan":
+        return run_scan_workload(args, rank, world)
+    if args.workload == "split":
+        return run_split_workload(args, rank, world)
 
     import numpy as np
     import torch

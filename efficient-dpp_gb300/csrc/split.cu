@@ -29,6 +29,7 @@
 // is stable, bit-identical to single_split (split_kernel.cl:676-736),
 // WG_split with FIXED_REORDER and the CUDA pre_scan/post_scan split.  There
 // are no inter-block waits.
+#include <algorithm>
 #include <mutex>
 
 #include "common.cuh"
@@ -54,8 +55,8 @@ template <int LAYOUT> __device__ __forceinline__ int32_t key_at(const int32_t *k
 // ---- stage 1: per-tile bucket counts ----------------------------------------
 template <int LAYOUT>
 __global__ void __launch_bounds__(kHistThreads)
-    split_hist_kernel(const int32_t *__restrict__ keys, int64_t n, int buckets, int64_t tiles,
-                      int32_t *__restrict__ his, bool vec) {
+    split_hist_kernel(const int32_t *__restrict__ keys, int64_t n, int buckets, int shift,
+                      int64_t tiles, int32_t *__restrict__ his, bool vec) {
   __shared__ uint32_t cnt[kMaxBuckets];
   const unsigned mask = static_cast<unsigned>(buckets - 1);
   for (int b = threadIdx.x; b < buckets; b += kHistThreads) cnt[b] = 0;
@@ -66,7 +67,7 @@ __global__ void __launch_bounds__(kHistThreads)
   const unsigned lt = lanemask_lt();
 
   auto add = [&](bool valid, int32_t key) {
-    const int b = valid ? static_cast<int>(static_cast<unsigned>(key) & mask) : -1;
+    const int b = valid ? static_cast<int>((static_cast<unsigned>(key) >> shift) & mask) : -1;
     const unsigned peers = __match_any_sync(0xffffffffu, b);
     if (valid && (peers & lt) == 0u) atomicAdd(&cnt[b], static_cast<uint32_t>(__popc(peers)));
   };
@@ -121,8 +122,9 @@ template <int THREADS, int LAYOUT>
 __global__ void __launch_bounds__(THREADS)
     split_scatter_kernel(const int32_t *__restrict__ keys_in, int32_t *__restrict__ keys_out,
                          const int32_t *__restrict__ vals_in, int32_t *__restrict__ vals_out,
-                         int64_t n, int buckets, int64_t tiles, const int32_t *__restrict__ his,
-                         bool tma, uint64_t timeout_ns, unsigned *fault) {
+                         int64_t n, int buckets, int shift, int64_t tiles,
+                         const int32_t *__restrict__ his, bool tma, uint64_t timeout_ns,
+                         unsigned *fault) {
   using C = ScatterCfg<THREADS>;
   constexpr bool kKV = LAYOUT != EDPP_KO;
   extern __shared__ __align__(128) unsigned char smem[];
@@ -199,7 +201,7 @@ __global__ void __launch_bounds__(THREADS)
         if (LAYOUT == EDPP_KVS_SOA) val = s_vals[pos];
       }
     }
-    const int b = valid ? static_cast<int>(static_cast<unsigned>(key) & mask) : -1;
+    const int b = valid ? static_cast<int>((static_cast<unsigned>(key) >> shift) & mask) : -1;
     const unsigned peers = __match_any_sync(0xffffffffu, b);
     const unsigned lower = peers & lt;
     const uint16_t before = valid ? my_cnt[b] : 0;
@@ -267,7 +269,7 @@ __global__ void __launch_bounds__(THREADS)
   for (int it = 0; it < C::kIters; ++it) {
     const int pos = w * C::kSeg + it * 32 + lane;
     if (pos < count) {
-      const int b = static_cast<int>(static_cast<unsigned>(kk[it]) & mask);
+      const int b = static_cast<int>((static_cast<unsigned>(kk[it]) >> shift) & mask);
       const int r = static_cast<int>((rk[it >> 1] >> ((it & 1) * 16)) & 0xffffu);
       const int s = toff[b] + cnt16[w * buckets + b] + r;
       if (LAYOUT == EDPP_KVS_AOS) {
@@ -284,11 +286,11 @@ __global__ void __launch_bounds__(THREADS)
   for (int s = tid; s < count; s += THREADS) {
     if (LAYOUT == EDPP_KVS_AOS) {
       const int2 p = s_pairs[s];
-      const int b = static_cast<int>(static_cast<unsigned>(p.x) & mask);
+      const int b = static_cast<int>((static_cast<unsigned>(p.x) >> shift) & mask);
       reinterpret_cast<int2 *>(keys_out)[gofs[b] + s] = p;
     } else {
       const int32_t key = s_keys[s];
-      const int b = static_cast<int>(static_cast<unsigned>(key) & mask);
+      const int b = static_cast<int>((static_cast<unsigned>(key) >> shift) & mask);
       const int64_t o = static_cast<int64_t>(gofs[b]) + s;
       keys_out[o] = key;
       if (LAYOUT == EDPP_KVS_SOA) vals_out[o] = s_vals[s];
@@ -324,13 +326,13 @@ template <int THREADS, int LAYOUT> int set_smem_attr() {
 
 template <int THREADS, int LAYOUT>
 int launch_scatter(const int32_t *keys_in, int32_t *keys_out, const int32_t *vals_in,
-                   int32_t *vals_out, int64_t n, int buckets, int64_t tiles, const int32_t *his,
-                   bool tma, cudaStream_t st) {
+                   int32_t *vals_out, int64_t n, int buckets, int shift, int64_t tiles,
+                   const int32_t *his, bool tma, cudaStream_t st) {
   const int s = set_smem_attr<THREADS, LAYOUT>();
   if (s != EDPP_OK) return s;
   const size_t smem = scatter_smem_bytes<THREADS, LAYOUT>(buckets);
   split_scatter_kernel<THREADS, LAYOUT><<<static_cast<unsigned>(tiles), THREADS, smem, st>>>(
-      keys_in, keys_out, vals_in, vals_out, n, buckets, tiles, his, tma, kDefaultWaitNs,
+      keys_in, keys_out, vals_in, vals_out, n, buckets, shift, tiles, his, tma, kDefaultWaitNs,
       fault_word());
   return launch_status();
 }
@@ -338,7 +340,7 @@ int launch_scatter(const int32_t *keys_in, int32_t *keys_out, const int32_t *val
 template <int LAYOUT>
 int split_layout(const int32_t *keys_in, int32_t *keys_out, int32_t *bucket_start, int64_t n,
                  int buckets, const int32_t *vals_in, int32_t *vals_out, void *ws, size_t ws_bytes,
-                 cudaStream_t st) {
+                 cudaStream_t st, int shift = 0) {
   const int64_t tiles = (n + kTile - 1) / kTile;
   int32_t *his = static_cast<int32_t *>(ws);
   const int64_t hlen = tiles * buckets;
@@ -346,7 +348,7 @@ int split_layout(const int32_t *keys_in, int32_t *keys_out, int32_t *bucket_star
   const size_t scan_ws_bytes = ws_bytes - his_bytes(tiles, buckets);
   bool tma = aligned16(keys_in) && (LAYOUT != EDPP_KVS_SOA || aligned16(vals_in));
   split_hist_kernel<LAYOUT><<<static_cast<unsigned>(tiles), kHistThreads, 0, st>>>(
-      keys_in, n, buckets, tiles, his, aligned16(keys_in));
+      keys_in, n, buckets, shift, tiles, his, aligned16(keys_in));
   int s = launch_status();
   if (s != EDPP_OK) return s;
   s = edpp_scan_exclusive_i32(his, his, hlen, EDPP_SCAN_LOOKBACK, scan_ws, scan_ws_bytes, st);
@@ -357,10 +359,10 @@ int split_layout(const int32_t *keys_in, int32_t *keys_out, int32_t *bucket_star
     if (s != EDPP_OK) return s;
   }
   if (buckets <= 1024)
-    return launch_scatter<512, LAYOUT>(keys_in, keys_out, vals_in, vals_out, n, buckets, tiles, his,
-                                       tma, st);
-  return launch_scatter<256, LAYOUT>(keys_in, keys_out, vals_in, vals_out, n, buckets, tiles, his,
-                                     tma, st);
+    return launch_scatter<512, LAYOUT>(keys_in, keys_out, vals_in, vals_out, n, buckets, shift,
+                                       tiles, his, tma, st);
+  return launch_scatter<256, LAYOUT>(keys_in, keys_out, vals_in, vals_out, n, buckets, shift,
+                                     tiles, his, tma, st);
 }
 
 size_t split_ws_bytes(int64_t n, int buckets) {
@@ -408,3 +410,71 @@ int edpp_split_i32(const int32_t *keys_in, int32_t *keys_out, int32_t *bucket_st
 }
 
 }  // extern "C"
+
+// ---- LSD radix sort on the stable split -----------------------------------------
+// Sorts (key, value) pairs by the key's bit pattern (unsigned order) over bits
+// [begin_bit, end_bit), 8 bits per pass, each pass one stable split by the
+// digit (key >> shift) & 255, ping-ponging through the workspace; the last
+// pass lands in the caller's output.  Follows the reference's LSD radix sort
+// (obsolete/CUDA/kernels/radixSort.cu:333-357: histogram, scan, scatter per
+// digit over all bits of the key), with the GB300 split as the per-digit pass.
+namespace {
+
+size_t radix_ws_bytes(int64_t n, bool with_values) {
+  const size_t buf = edpp::round_up(static_cast<size_t>(n) * 4, 256);
+  return buf * (with_values ? 2 : 1) + edpp::split_ws_bytes(n, 256);
+}
+
+}  // namespace
+
+extern "C" size_t edpp_radix_sort_workspace_size(int64_t length, int with_values) {
+  if (length <= 0) return 0;
+  return radix_ws_bytes(length, with_values != 0);
+}
+
+extern "C" int edpp_radix_sort_i32(const int32_t *keys_in, int32_t *keys_out,
+                                   const int32_t *vals_in, int32_t *vals_out, int64_t length,
+                                   int begin_bit, int end_bit, void *ws, size_t ws_bytes,
+                                   void *stream) {
+  using namespace edpp;
+  if (length < 0 || length > INT32_MAX) return EDPP_EINVAL;
+  if (begin_bit < 0 || end_bit > 32 || begin_bit > end_bit) return EDPP_EINVAL;
+  const bool kv = vals_in != nullptr;
+  if (kv && !vals_out) return EDPP_EINVAL;
+  if (length == 0) return EDPP_OK;
+  if (!keys_in || !keys_out || keys_in == keys_out || (kv && vals_in == vals_out))
+    return EDPP_EINVAL;
+  if (!ws || ws_bytes < radix_ws_bytes(length, kv)) return EDPP_ENOMEM;
+  cudaStream_t st = as_stream(stream);
+  const size_t bytes = static_cast<size_t>(length) * 4;
+  if (begin_bit == end_bit) {  // no digit: a copy
+    if (cudaMemcpyAsync(keys_out, keys_in, bytes, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+      return EDPP_ECUDA;
+    if (kv && cudaMemcpyAsync(vals_out, vals_in, bytes, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+      return EDPP_ECUDA;
+    return EDPP_OK;
+  }
+  const size_t buf = round_up(bytes, 256);
+  char *w = static_cast<char *>(ws);
+  int32_t *tk = reinterpret_cast<int32_t *>(w);
+  int32_t *tv = kv ? reinterpret_cast<int32_t *>(w + buf) : nullptr;
+  void *sws = w + buf * (kv ? 2 : 1);
+  const size_t sws_bytes = ws_bytes - buf * (kv ? 2 : 1);
+  const int passes = (end_bit - begin_bit + 7) / 8;
+  const int32_t *sk = keys_in, *sv = vals_in;
+  for (int i = 0; i < passes; ++i) {
+    const int shift = begin_bit + 8 * i;
+    const int bits = std::min(8, end_bit - shift);
+    const bool to_out = ((passes - 1 - i) % 2) == 0;
+    int32_t *dk = to_out ? keys_out : tk;
+    int32_t *dv = kv ? (to_out ? vals_out : tv) : nullptr;
+    const int s = kv ? split_layout<EDPP_KVS_SOA>(sk, dk, nullptr, length, 1 << bits, sv, dv, sws,
+                                                  sws_bytes, st, shift)
+                     : split_layout<EDPP_KO>(sk, dk, nullptr, length, 1 << bits, nullptr, nullptr,
+                                             sws, sws_bytes, st, shift);
+    if (s != EDPP_OK) return s;
+    sk = dk;
+    sv = dv;
+  }
+  return EDPP_OK;
+}

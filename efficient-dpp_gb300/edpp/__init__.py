@@ -55,6 +55,8 @@ SIGNATURES = {
     "edpp_scan_inclusive_f32": (_I, [_VP, _VP, _I64, _I, _VP, _SZ, _VP]),
     "edpp_split_workspace_size": (_SZ, [_I64, _I, _I]),
     "edpp_split_i32": (_I, [_VP, _VP, _VP, _I64, _I, _I, _VP, _VP, _VP, _SZ, _VP]),
+    "edpp_radix_sort_workspace_size": (_SZ, [_I64, _I]),
+    "edpp_radix_sort_i32": (_I, [_VP, _VP, _VP, _VP, _I64, _I, _I, _VP, _SZ, _VP]),
     "edpp_stream_copy_f32": (_I, [_VP, _VP, _I64, _VP]),
     "edpp_stream_scale_f32": (_I, [_VP, _VP, _F, _I64, _VP]),
     "edpp_stream_add_f32": (_I, [_VP, _VP, _VP, _I64, _VP]),
@@ -272,6 +274,27 @@ def split(keys, buckets: int, values=None, layout: str | None = None, bucket_sta
                                _p(values_out if layout == "soa" else None), _p(ws), ws.numel(),
                                current_stream_handle()), "split")
     return keys_out, (values_out if layout == "soa" else None), start
+
+
+def radix_sort(keys, values=None, begin_bit=0, end_bit=32, keys_out=None, values_out=None,
+               ws=None):
+    """Stable LSD radix sort by the key's bit pattern (unsigned order)."""
+    torch = _torch()
+    _cuda_tensor(keys, torch.int32, "keys")
+    n = keys.numel()
+    if keys_out is None:
+        keys_out = torch.empty_like(keys)
+    if values is not None:
+        _cuda_tensor(values, torch.int32, "values")
+        if values_out is None:
+            values_out = torch.empty_like(values)
+    if ws is None:
+        ws = workspace(lib().edpp_radix_sort_workspace_size(n, int(values is not None)),
+                       keys.device)
+    check(lib().edpp_radix_sort_i32(_p(keys), _p(keys_out), _p(values), _p(values_out), n,
+                                    int(begin_bit), int(end_bit), _p(ws), ws.numel(),
+                                    current_stream_handle()), "radix_sort")
+    return keys_out, values_out
 
 
 def stream(op: str, a, b=None, scalar=3, out=None):

@@ -186,6 +186,19 @@ int edpp_split_i32(const int32_t *keys_in, int32_t *keys_out,
                    int layout, const int32_t *vals_in, int32_t *vals_out,
                    void *ws, size_t ws_bytes, void *stream);
 
+/* ---- radix sort on the stable split -------------------------------------- */
+
+/* LSD radix sort of int32 keys (with optional int32 values) by the key's bit
+ * pattern (unsigned order) over bits [begin_bit, end_bit), 8 bits per pass,
+ * each pass one stable split; stable.  keys_in != keys_out.  vals_in NULL:
+ * keys only.  Counterpart of the reference's LSD radix sort
+ * (obsolete/CUDA/kernels/radixSort.cu:29-370), the main consumer of split. */
+size_t edpp_radix_sort_workspace_size(int64_t length, int with_values);
+int edpp_radix_sort_i32(const int32_t *keys_in, int32_t *keys_out,
+                        const int32_t *vals_in, int32_t *vals_out, int64_t length,
+                        int begin_bit, int end_bit, void *ws, size_t ws_bytes,
+                        void *stream);
+
 /* ---- STREAM ------------------------------------------------------------- */
 
 /* copy c=a, scale c=s*a, add c=a+b, triad c=a+s*b.  Replace the kernels of
