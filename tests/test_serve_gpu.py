@@ -75,10 +75,16 @@ def test_alone_equals_mix_equals_oracle(cuda, edpp, serve):
     e0, e1 = reference_outputs(segs, in0, in1)
     with serve.Server(pool_bytes=256 << 20, slots=3) as srv:
         alone, _ = _run(srv, serve, reqs, concurrent=False)
+        mix3, _ = _run(srv, serve, reqs, concurrent=True)
+        assert srv.stats()["completed"] == 2 * len(reqs)
+    # one slot: requests arriving while a batch runs queue up and are
+    # admitted together into the next batch
+    with serve.Server(pool_bytes=256 << 20, slots=1) as srv:
         mix, lat = _run(srv, serve, reqs, concurrent=True)
         stats = srv.stats()
-    assert stats["completed"] == 2 * len(reqs)
-    assert stats["max_requests_per_batch"] > 1  # requests were batched together
+    for i in range(len(reqs)):
+        np.testing.assert_array_equal(mix3[i][0], mix[i][0])
+        np.testing.assert_array_equal(mix3[i][1], mix[i][1])
     for i, s in enumerate(segs):
         o, L, op = int(s["offset"]), int(s["length"]), int(s["op"])
         np.testing.assert_array_equal(alone[i][0], mix[i][0])
@@ -87,6 +93,8 @@ def test_alone_equals_mix_equals_oracle(cuda, edpp, serve):
             np.testing.assert_array_equal(alone[i][1], mix[i][1])
             np.testing.assert_array_equal(alone[i][1], e1[o:o + L])
     assert all(x > 0 for x in lat)
+    assert stats["completed"] == len(reqs)
+    assert stats["max_requests_per_batch"] > 1  # requests were batched together
 
 
 def test_admission_waits_for_memory(cuda, edpp, serve):
