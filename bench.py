@@ -271,7 +271,7 @@ def run_batch_workload(args, rank, world):
     edpp.lib()
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
     torch.cuda.set_device(dev)
-    segs = B.config5_segments()
+    segs = B.config5_segments(cap=1 << args.batch_log2_total)
     in0, in1 = B.gen_inputs(segs, seed=4)
     n = len(in0)
     elems = int(segs["length"].sum())
@@ -610,6 +610,8 @@ def main(argv=None):
     ap.add_argument("--serve-payloads", type=int, default=48)
     ap.add_argument("--serve-slots", type=int, default=4)
     ap.add_argument("--pool-gb", type=float, default=40.0)
+    ap.add_argument("--batch-log2-total", type=int, default=30,
+                    help="batch: cap on the total elements (2^30 in the config)")
     ap.add_argument("--scan-log2n", type=int, default=30)
     ap.add_argument("--split-log2n", type=int, default=28)
     ap.add_argument("--autotune", action="store_true",

@@ -60,6 +60,8 @@ union __align__(128) BatchSmem {
   struct {
     int32_t keys[kTile];
     int32_t vals[kTile];
+    int32_t okeys[kTile];  // the tile re-laid out in bucket order
+    int32_t ovals[kTile];
     uint16_t cnt16[kWarps * kMaxB];
     int32_t toff[kMaxB];
     int32_t gofs[kMaxB];
@@ -105,13 +107,14 @@ __device__ void block_exclusive_scan_inplace(int32_t *p, int64_t m, int32_t *wsu
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 3)
     batch_kernel(const DevSeg *__restrict__ segs, const DevTask *__restrict__ tasks, int num_tasks,
                  const int32_t *__restrict__ in0, const int32_t *__restrict__ in1,
                  int32_t *__restrict__ out0, int32_t *__restrict__ out1, char *state,
                  Ctrl *ctrl, unsigned long long *ticket, unsigned *abort_flag, bool tma,
                  uint64_t timeout_ns, unsigned *fault) {
-  __shared__ BatchSmem sm;
+  extern __shared__ __align__(128) unsigned char batch_smem[];
+  BatchSmem &sm = *reinterpret_cast<BatchSmem *>(batch_smem);
   __shared__ alignas(8) uint64_t bar;
   __shared__ int s_task;
   __shared__ int s_flag;
@@ -123,9 +126,18 @@ __global__ void __launch_bounds__(kThreads)
   __syncthreads();
   uint32_t phase = 0;
   const unsigned lt = lanemask_lt_b();
+  // Thread 0 keeps the next ticket in hand while the block works on the
+  // current task, hiding the atomic's latency.  A block's current task never
+  // waits on its own prefetched task (waits only target earlier tickets),
+  // and tickets are handed out in order, so progress is unaffected.
+  int next_task = 0;
+  if (t == 0) next_task = static_cast<int>(atomicAdd(ticket, 1ull));
 
   while (true) {
-    if (t == 0) s_task = static_cast<int>(atomicAdd(ticket, 1ull));
+    if (t == 0) {
+      s_task = next_task;
+      if (next_task < num_tasks) next_task = static_cast<int>(atomicAdd(ticket, 1ull));
+    }
     __syncthreads();
     const int task_id = s_task;
     if (task_id >= num_tasks) break;
@@ -169,22 +181,20 @@ __global__ void __launch_bounds__(kThreads)
     } else if (task.kind == kTaskGather) {
       // ---- permutation gather tile, indices local to the segment ----
       const int32_t *src = in0 + seg.off;
+      constexpr int kPerT = kTile / kThreads;  // 16: every load in flight at once
+      int v[kPerT], idx[kPerT];
 #pragma unroll
-      for (int k = 0; k < kTile / kThreads; k += 4) {
-        int v[4], idx[4];
+      for (int q = 0; q < kPerT; ++q) {
+        const int i = q * kThreads + t;
+        idx[q] = i < count ? in1[gbase + i] : -1;
+      }
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int i = (k + q) * kThreads + t;
-          idx[q] = i < count ? in1[gbase + i] : -1;
-        }
+      for (int q = 0; q < kPerT; ++q)
+        v[q] = (idx[q] >= 0 && idx[q] < seg.len) ? __ldg(src + idx[q]) : 0;
 #pragma unroll
-        for (int q = 0; q < 4; ++q)
-          v[q] = (idx[q] >= 0 && idx[q] < seg.len) ? __ldg(src + idx[q]) : 0;
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int i = (k + q) * kThreads + t;
-          if (idx[q] >= 0 && idx[q] < seg.len) out0[gbase + i] = v[q];
-        }
+      for (int q = 0; q < kPerT; ++q) {
+        const int i = q * kThreads + t;
+        if (idx[q] >= 0 && idx[q] < seg.len) out0[gbase + i] = v[q];
       }
     } else if (task.kind == kTaskHist) {
       // ---- bucket counts of a split tile ----
@@ -246,14 +256,12 @@ __global__ void __launch_bounds__(kThreads)
         for (int i = t; i < kWarps * B; i += kThreads) sm.split.cnt16[i] = 0;
         __syncthreads();
         uint16_t *my = sm.split.cnt16 + w * B;
-        int32_t kk[kIters], vv[kIters];
         uint32_t rk[kIters / 2];
 #pragma unroll
         for (int it = 0; it < kIters; ++it) {
           const int pos = w * kSeg + it * 32 + lane;
           const bool valid = pos < count;
           const int32_t key = valid ? sm.split.keys[pos] : 0;
-          const int32_t val = valid ? sm.split.vals[pos] : 0;
           const int b = valid ? static_cast<int>(static_cast<unsigned>(key) & mask) : -1;
           const unsigned peers = __match_any_sync(0xffffffffu, b);
           const unsigned lower = peers & lt;
@@ -261,8 +269,6 @@ __global__ void __launch_bounds__(kThreads)
           __syncwarp();
           if (valid && lower == 0u) my[b] = static_cast<uint16_t>(before + __popc(peers));
           __syncwarp();
-          kk[it] = key;
-          vv[it] = val;
           const uint32_t r = static_cast<uint32_t>(before + __popc(lower));
           if (it & 1) rk[it >> 1] |= r << 16;
           else rk[it >> 1] = r;
@@ -300,20 +306,21 @@ __global__ void __launch_bounds__(kThreads)
         for (int it = 0; it < kIters; ++it) {
           const int pos = w * kSeg + it * 32 + lane;
           if (pos < count) {
-            const int b = static_cast<int>(static_cast<unsigned>(kk[it]) & mask);
+            const int32_t key = sm.split.keys[pos];
+            const int b = static_cast<int>(static_cast<unsigned>(key) & mask);
             const int r = static_cast<int>((rk[it >> 1] >> ((it & 1) * 16)) & 0xffffu);
             const int s = sm.split.toff[b] + sm.split.cnt16[w * B + b] + r;
-            sm.split.keys[s] = kk[it];
-            sm.split.vals[s] = vv[it];
+            sm.split.okeys[s] = key;
+            sm.split.ovals[s] = sm.split.vals[pos];
           }
         }
         __syncthreads();
         for (int s = t; s < count; s += kThreads) {
-          const int32_t key = sm.split.keys[s];
+          const int32_t key = sm.split.okeys[s];
           const int b = static_cast<int>(static_cast<unsigned>(key) & mask);
           const int64_t o = seg.off + sm.split.gofs[b] + s;
           out0[o] = key;
-          out1[o] = sm.split.vals[s];
+          out1[o] = sm.split.ovals[s];
         }
       }
     }
@@ -487,7 +494,17 @@ int edpp_batch_launch(const edpp_batch_plan *plan, const int32_t *in0, const int
   const int sms = device_sm_count();
   int64_t blocks = static_cast<int64_t>(sms) * p.blocks_per_sm;
   blocks = min64(blocks, static_cast<int64_t>(p.tasks.size()));
-  batch_kernel<<<static_cast<unsigned>(max64(blocks, 1)), kThreads, 0, st>>>(
+  static std::once_flag attr_once[64];
+  static cudaError_t attr_err[64];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  std::call_once(attr_once[dev], [dev] {
+    attr_err[dev] = cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(sizeof(BatchSmem)));
+  });
+  if (attr_err[dev] != cudaSuccess) return EDPP_ECUDA;
+  batch_kernel<<<static_cast<unsigned>(max64(blocks, 1)), kThreads, sizeof(BatchSmem), st>>>(
       reinterpret_cast<const DevSeg *>(w + p.off_segs),
       reinterpret_cast<const DevTask *>(w + p.off_tasks), static_cast<int>(p.tasks.size()), in0,
       in1, out0, out1, w + p.off_state, reinterpret_cast<Ctrl *>(w + p.off_ctrl),

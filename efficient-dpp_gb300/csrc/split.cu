@@ -478,3 +478,99 @@ extern "C" int edpp_radix_sort_i32(const int32_t *keys_in, int32_t *keys_out,
   }
   return EDPP_OK;
 }
+
+// ---- WI_split order -----------------------------------------------------------------
+// The reference's WI_split (opencl/kernels/split_kernel.cl:335-412, with
+// compute_mixed_access, scan_global_RSS_kernel.cl:37-48) gives work-item
+// g = chunk*step + lane the indices chunk*C + lane + step*k of its chunk
+// (C = step*tile, step = min(local_size, 32), tile = ceil(n / (local_size *
+// grid_size))) and writes them bucket-major, then by g, then by k.  That is
+// the stable split of the input visited in (chunk, lane, k) order, so this
+// mode gathers the input into that order and runs the stable split.  With
+// tile == 1 (n <= local_size*grid_size) the order is the stable order.
+namespace edpp {
+namespace {
+
+template <int LAYOUT>
+__global__ void wi_permute_kernel(const int32_t *__restrict__ keys, const int32_t *__restrict__ vals,
+                                  int32_t *__restrict__ tk, int32_t *__restrict__ tv, int64_t n,
+                                  int64_t chunk, int64_t step) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; j < n; j += stride) {
+    const int64_t c = j / chunk, r = j - c * chunk;
+    const int64_t len = min64(chunk, n - c * chunk);
+    const int64_t base = len / step, rem = len % step;
+    int64_t lane, k;
+    if (r < rem * (base + 1)) {
+      lane = r / (base + 1);
+      k = r - lane * (base + 1);
+    } else {
+      const int64_t r2 = r - rem * (base + 1);
+      lane = rem + r2 / base;
+      k = r2 - (lane - rem) * base;
+    }
+    const int64_t i = c * chunk + lane + step * k;
+    if (LAYOUT == EDPP_KVS_AOS) {
+      tk[2 * j] = keys[2 * i];
+      tk[2 * j + 1] = keys[2 * i + 1];
+    } else {
+      tk[j] = keys[i];
+      if (LAYOUT == EDPP_KVS_SOA) tv[j] = vals[i];
+    }
+  }
+}
+
+size_t wi_tmp_bytes(int64_t n, int layout) {
+  const size_t one = round_up(static_cast<size_t>(n) * 4, 256);
+  return layout == EDPP_KO ? one : 2 * one;
+}
+
+}  // namespace
+}  // namespace edpp
+
+extern "C" size_t edpp_split_wi_workspace_size(int64_t length, int buckets, int layout) {
+  const size_t sw = edpp_split_workspace_size(length, buckets, layout);
+  if (sw == 0) return 0;
+  return edpp::wi_tmp_bytes(length, layout) + sw;
+}
+
+extern "C" int edpp_split_i32_wi(const int32_t *keys_in, int32_t *keys_out, int64_t length,
+                                 int buckets, int layout, const int32_t *vals_in,
+                                 int32_t *vals_out, int local_size, int grid_size, void *ws,
+                                 size_t ws_bytes, void *stream) {
+  using namespace edpp;
+  if (local_size < 1 || grid_size < 1) return EDPP_EINVAL;
+  if (length < 0 || length > INT32_MAX) return EDPP_EINVAL;
+  if (buckets < 1 || buckets > kMaxBuckets || (buckets & (buckets - 1))) return EDPP_EINVAL;
+  if (layout != EDPP_KO && layout != EDPP_KVS_AOS && layout != EDPP_KVS_SOA) return EDPP_EINVAL;
+  if (length == 0) return EDPP_OK;
+  if (!keys_in || !keys_out) return EDPP_EINVAL;
+  if (layout == EDPP_KVS_SOA && (!vals_in || !vals_out)) return EDPP_EINVAL;
+  const int64_t G = static_cast<int64_t>(local_size) * grid_size;
+  const int64_t step = local_size < 32 ? local_size : 32;
+  const int64_t tile = (length + G - 1) / G;
+  const size_t tmp = wi_tmp_bytes(length, layout);
+  if (!ws || ws_bytes < tmp + edpp_split_workspace_size(length, buckets, layout)) return EDPP_ENOMEM;
+  if (tile == 1)
+    return edpp_split_i32(keys_in, keys_out, nullptr, length, buckets, layout, vals_in, vals_out,
+                          static_cast<char *>(ws) + tmp, ws_bytes - tmp, stream);
+  cudaStream_t st = as_stream(stream);
+  int32_t *tk = static_cast<int32_t *>(ws);
+  int32_t *tv = layout == EDPP_KVS_SOA
+                    ? reinterpret_cast<int32_t *>(static_cast<char *>(ws) + tmp / 2)
+                    : nullptr;
+  const unsigned blocks = static_cast<unsigned>(min64((length + 255) / 256, device_sm_count() * 8));
+  if (layout == EDPP_KO)
+    wi_permute_kernel<EDPP_KO><<<blocks, 256, 0, st>>>(keys_in, nullptr, tk, nullptr, length,
+                                                        step * tile, step);
+  else if (layout == EDPP_KVS_SOA)
+    wi_permute_kernel<EDPP_KVS_SOA><<<blocks, 256, 0, st>>>(keys_in, vals_in, tk, tv, length,
+                                                             step * tile, step);
+  else
+    wi_permute_kernel<EDPP_KVS_AOS><<<blocks, 256, 0, st>>>(keys_in, nullptr, tk, nullptr, length,
+                                                             step * tile, step);
+  const int s = launch_status();
+  if (s != EDPP_OK) return s;
+  return edpp_split_i32(tk, keys_out, nullptr, length, buckets, layout, tv, vals_out,
+                        static_cast<char *>(ws) + tmp, ws_bytes - tmp, stream);
+}

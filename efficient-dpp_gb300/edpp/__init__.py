@@ -55,6 +55,8 @@ SIGNATURES = {
     "edpp_scan_inclusive_f32": (_I, [_VP, _VP, _I64, _I, _VP, _SZ, _VP]),
     "edpp_split_workspace_size": (_SZ, [_I64, _I, _I]),
     "edpp_split_i32": (_I, [_VP, _VP, _VP, _I64, _I, _I, _VP, _VP, _VP, _SZ, _VP]),
+    "edpp_split_wi_workspace_size": (_SZ, [_I64, _I, _I]),
+    "edpp_split_i32_wi": (_I, [_VP, _VP, _I64, _I, _I, _VP, _VP, _I, _I, _VP, _SZ, _VP]),
     "edpp_radix_sort_workspace_size": (_SZ, [_I64, _I]),
     "edpp_radix_sort_i32": (_I, [_VP, _VP, _VP, _VP, _I64, _I, _I, _VP, _SZ, _VP]),
     "edpp_stream_copy_f32": (_I, [_VP, _VP, _I64, _VP]),
@@ -274,6 +276,24 @@ def split(keys, buckets: int, values=None, layout: str | None = None, bucket_sta
                                _p(values_out if layout == "soa" else None), _p(ws), ws.numel(),
                                current_stream_handle()), "split")
     return keys_out, (values_out if layout == "soa" else None), start
+
+
+def split_wi(keys, buckets, values=None, layout=None, local_size=256, grid_size=32768):
+    """The reference WI_split's order (see edpp_split_i32_wi)."""
+    torch = _torch()
+    if layout is None:
+        layout = "ko" if values is None else "soa"
+    _cuda_tensor(keys, torch.int32, "keys")
+    n = keys.shape[0]
+    ko = torch.empty_like(keys)
+    vo = torch.empty_like(values) if layout == "soa" else None
+    ws = workspace(lib().edpp_split_wi_workspace_size(n, int(buckets), LAYOUTS[layout]),
+                   keys.device)
+    check(lib().edpp_split_i32_wi(_p(keys), _p(ko), n, int(buckets), LAYOUTS[layout],
+                                  _p(values if layout == "soa" else None), _p(vo),
+                                  int(local_size), int(grid_size), _p(ws), ws.numel(),
+                                  current_stream_handle()), "split_wi")
+    return ko, vo
 
 
 def radix_sort(keys, values=None, begin_bit=0, end_bit=32, keys_out=None, values_out=None,

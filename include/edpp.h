@@ -186,6 +186,19 @@ int edpp_split_i32(const int32_t *keys_in, int32_t *keys_out,
                    int layout, const int32_t *vals_in, int32_t *vals_out,
                    void *ws, size_t ws_bytes, void *stream);
 
+/* WI_split's own output order (bit-exact with the reference's WI_split for
+ * the given local_size / grid_size; opencl/primitives/splitImpl.cpp:21-142,
+ * split_kernel.cl:335-412): elements by bucket, then by work-item, then in
+ * each work-item's lane-strided visiting order.  Equals the stable order when
+ * length <= local_size * grid_size.  (The reference's d_start output of
+ * WI_split indexes its per-work-item histogram with the per-group stride, so
+ * it has no bucket-start meaning; use edpp_split_i32's bucket_start.) */
+size_t edpp_split_wi_workspace_size(int64_t length, int buckets, int layout);
+int edpp_split_i32_wi(const int32_t *keys_in, int32_t *keys_out, int64_t length,
+                      int buckets, int layout, const int32_t *vals_in, int32_t *vals_out,
+                      int local_size, int grid_size, void *ws, size_t ws_bytes,
+                      void *stream);
+
 /* ---- radix sort on the stable split -------------------------------------- */
 
 /* LSD radix sort of int32 keys (with optional int32 values) by the key's bit

@@ -457,3 +457,55 @@ double orc_average_hampel(const double *x, int n) {
   free(ds);
   return valid ? total / valid : 0.0;
 }
+
+/* ---- literal restatement of the OpenCL WI_split order --------------------------
+ * WI_histogram / WI_shuffle (opencl/kernels/split_kernel.cl:335-412) with
+ * compute_mixed_access (scan_global_RSS_kernel.cl:37-48): work-item g of G =
+ * local_size * grid_size, step = min(local_size, 32), tile = ceil(n / G),
+ * warp = g / step, begin = warp*step*tile + g%step, end = min((warp+1)*step*tile, n);
+ * g visits i = begin, begin+step, ... < end.  Histogram his[b*G + g], exclusive
+ * scan over (b, g), then each g writes its elements at his[b*G + g]++ in
+ * visiting order.  aos != 0: int32 pairs keyed on the first. */
+void orc_split_wi(const int32_t *in, const int32_t *vals, int64_t n, int buckets, int aos,
+                  int local_size, int grid_size, int32_t *out, int32_t *vals_out) {
+  const uint32_t mask = (uint32_t)buckets - 1u;
+  const int64_t G = (int64_t)local_size * grid_size;
+  const int64_t step = local_size < 32 ? local_size : 32;
+  const int64_t tile = (n + G - 1) / G;
+  int64_t *his = (int64_t *)calloc((size_t)(buckets * G), sizeof(int64_t));
+  if (!his) return;
+  for (int64_t g = 0; g < G; ++g) {
+    const int64_t warp = g / step;
+    const int64_t begin = warp * step * tile + (g % step);
+    int64_t end = (warp + 1) * step * tile;
+    if (end > n) end = n;
+    for (int64_t i = begin; i < end; i += step) {
+      const uint32_t b = (uint32_t)(aos ? in[2 * i] : in[i]) & mask;
+      his[(int64_t)b * G + g]++;
+    }
+  }
+  int64_t acc = 0;
+  for (int64_t k = 0; k < (int64_t)buckets * G; ++k) {
+    const int64_t v = his[k];
+    his[k] = acc;
+    acc += v;
+  }
+  for (int64_t g = 0; g < G; ++g) {
+    const int64_t warp = g / step;
+    const int64_t begin = warp * step * tile + (g % step);
+    int64_t end = (warp + 1) * step * tile;
+    if (end > n) end = n;
+    for (int64_t i = begin; i < end; i += step) {
+      const uint32_t b = (uint32_t)(aos ? in[2 * i] : in[i]) & mask;
+      const int64_t p = his[(int64_t)b * G + g]++;
+      if (aos) {
+        out[2 * p] = in[2 * i];
+        out[2 * p + 1] = in[2 * i + 1];
+      } else {
+        out[p] = in[i];
+        if (vals) vals_out[p] = vals[i];
+      }
+    }
+  }
+  free(his);
+}

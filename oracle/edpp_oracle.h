@@ -66,6 +66,11 @@ void orc_split_cuda_ballot(const int32_t *keys, int64_t n, int bucket_bits, int3
  * with G groups (the reference uses 39). */
 void orc_split_single(const int32_t *in, int64_t n, int buckets, int aos, int groups,
                       int32_t *out);
+/* Literal restatement of the OpenCL WI_split order (per-work-item histograms,
+ * lane-strided visiting; opencl/kernels/split_kernel.cl:335-412).  vals may
+ * be NULL (KO); aos != 0: int32 pairs in `in`/`out`. */
+void orc_split_wi(const int32_t *in, const int32_t *vals, int64_t n, int buckets, int aos,
+                  int local_size, int grid_size, int32_t *out, int32_t *vals_out);
 /* Elapsed-ms timing of the stable split restatement (CPU baseline). */
 double orc_split_stable_timed(const int32_t *keys, const int32_t *vals, int64_t n, int buckets,
                               int layout, int32_t *keys_out, int32_t *vals_out);

@@ -35,6 +35,7 @@ _SIG = {
     "orc_split_cuda_ballot": (None, [_VP, _I64, _I, _VP]),
     "orc_split_single": (None, [_VP, _I64, _I, _I, _I, _VP]),
     "orc_split_stable_timed": (_D, [_VP, _VP, _I64, _I, _I, _VP, _VP]),
+    "orc_split_wi": (None, [_VP, _VP, _I64, _I, _I, _I, _I, _VP, _VP]),
     "orc_compute_bandwidth": (_D, [ctypes.c_uint64, _I, _D]),
     "orc_average_hampel": (_D, [_VP, _I]),
     "orc_max_threads": (_I, []),
@@ -179,6 +180,17 @@ def split_single(data, buckets, aos=False, groups=39):
     n = data.shape[0]
     lib().orc_split_single(_p(data), n, buckets, int(aos), groups, _p(out))
     return out
+
+
+def split_wi(keys, buckets, values=None, aos=False, local_size=256, grid_size=32768):
+    """The reference WI_split's output order (restated literally)."""
+    keys = _c(keys, np.int32)
+    out = np.empty_like(keys)
+    vals = _c(values, np.int32) if values is not None else None
+    vo = np.empty_like(vals) if vals is not None else None
+    lib().orc_split_wi(_p(keys), _p(vals), keys.shape[0], buckets, int(aos), local_size, grid_size,
+                       _p(out), _p(vo))
+    return out, vo
 
 
 def average_hampel(x):

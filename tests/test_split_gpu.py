@@ -102,3 +102,27 @@ def test_config3_full_size_properties(cuda, edpp):
         exp_start = torch.cumsum(counts, 0) - counts
         assert torch.equal(st.long(), exp_start)
         del kd, vd, ko, vo, b, same
+
+
+@pytest.mark.parametrize("layout", ["ko", "soa", "aos"])
+@pytest.mark.parametrize("n,local,grid", [(100003, 256, 32768), (100003, 32, 16), (77777, 64, 7),
+                                          (5000, 16, 3), (1 << 20, 256, 128)])
+@pytest.mark.parametrize("B", [2, 64, 1024])
+def test_wi_split_order(cuda, edpp, orc, layout, n, local, grid, B):
+    # the reference WI_split's lane-strided order, bit-exact with the
+    # literal restatement of WI_histogram / WI_shuffle
+    keys = edpp.gen_keys_uniform(n, 3)
+    vals = np.arange(n, dtype=np.int32)
+    if layout == "aos":
+        pairs = np.stack([keys, vals], axis=1)
+        ko, _ = edpp.split_wi(to_dev(pairs), B, layout="aos", local_size=local, grid_size=grid)
+        ek, _ = orc.split_wi(pairs, B, aos=True, local_size=local, grid_size=grid)
+        np.testing.assert_array_equal(to_host(ko), ek)
+    else:
+        v = vals if layout == "soa" else None
+        ko, vo = edpp.split_wi(to_dev(keys), B, None if v is None else to_dev(v), layout=layout,
+                               local_size=local, grid_size=grid)
+        ek, ev = orc.split_wi(keys, B, v, local_size=local, grid_size=grid)
+        np.testing.assert_array_equal(to_host(ko), ek)
+        if v is not None:
+            np.testing.assert_array_equal(to_host(vo), ev)
