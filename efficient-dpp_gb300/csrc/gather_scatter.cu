@@ -132,7 +132,9 @@ int multipass(const int32_t *in, int32_t *out, int64_t n, const int32_t *loc, in
   const bool vec = aligned16(loc) && aligned16(out) && (!kScatter || aligned16(in));
   const int64_t per_block = static_cast<int64_t>(kThreads) * 4 * kUnroll;
   int64_t blocks = (n + per_block - 1) / per_block;
-  const int64_t cap = static_cast<int64_t>(device_sm_count()) * 8;
+  // 16 resident blocks of 256 threads per SM: the random side is latency
+  // bound, so more independent loads in flight help (measured on GB300).
+  const int64_t cap = static_cast<int64_t>(device_sm_count()) * 16;
   if (blocks > cap) blocks = cap;
   if (blocks < 1) blocks = 1;
   // Window arithmetic of gatherImpl.cpp:38-44 (len_per_run = ceil(n/pass)).

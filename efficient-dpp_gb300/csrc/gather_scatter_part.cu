@@ -35,7 +35,6 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kPer = 16;                    // elements per thread per tile
 constexpr int kTile = kThreads * kPer;      // 4096
-constexpr int kWarpsP = kThreads / 32;
 constexpr int kMaxWin = 2048;               // windows
 constexpr int64_t kMinWin = 1024;           // elements per window, at least
 constexpr int kChunk = 8192;                // pairs per ticket in ordered sweeps
@@ -62,67 +61,6 @@ __device__ __forceinline__ int rank_in_window(int w, uint32_t *scnt, unsigned lt
   if (w >= 0 && (peers & lt) == 0u) base = atomicAdd(&scnt[w], static_cast<uint32_t>(__popc(peers)));
   base = __shfl_sync(0xffffffffu, base, leader);
   return w >= 0 ? static_cast<int>(base) + __popc(peers & lt) : -1;
-}
-
-// ---- ballot ranking (at most 64 windows) ----------------------------------------
-// For up to 64 windows, per-window lane masks come from one ballot per
-// window-index bit (the reference's warp_histogram idea,
-// cuda/test_split.cu:19-54): lane j can count window j's elements of a
-// 32-element slot, and every lane finds the lanes of its own window, without
-// __match_any_sync or per-element shared-memory atomics.
-constexpr int kBallotMaxWin = 64;
-
-__device__ __forceinline__ unsigned lanes_of_window(int j, unsigned vb, const unsigned (&bal)[6],
-                                                    int bits) {
-  unsigned m = vb;
-#pragma unroll
-  for (int k = 0; k < 6; ++k)
-    if (k < bits) m &= ((j >> k) & 1) ? bal[k] : ~bal[k];
-  return m;
-}
-
-// Rank of this lane's element among the warp's elements of its window so
-// far (-1: invalid).  run0 / run1: this lane's running counts of windows
-// `lane` and `lane + 32`.
-__device__ __forceinline__ int warp_rank_ballot(int w, int bits, bool two, unsigned lt, int lane,
-                                                uint32_t &run0, uint32_t &run1) {
-  const bool valid = w >= 0;
-  const unsigned vb = __ballot_sync(0xffffffffu, valid);
-  unsigned bal[6];
-#pragma unroll
-  for (int k = 0; k < 6; ++k) bal[k] = (k < bits) ? __ballot_sync(0xffffffffu, valid && ((w >> k) & 1)) : 0u;
-  const unsigned mine = valid ? lanes_of_window(w, vb, bal, bits) : 0u;
-  const uint32_t r0 = __shfl_sync(0xffffffffu, run0, w & 31);
-  const uint32_t r1 = two ? __shfl_sync(0xffffffffu, run1, w & 31) : 0u;
-  const int rank = valid ? static_cast<int>((w < 32 ? r0 : r1) + __popc(mine & lt)) : -1;
-  run0 += __popc(lanes_of_window(lane, vb, bal, bits));
-  if (two) run1 += __popc(lanes_of_window(lane + 32, vb, bal, bits));
-  return rank;
-}
-
-// Per-warp window counts -> tile counts scnt[] and per-(warp, window) bases.
-__device__ __forceinline__ void ballot_tile_counts(uint32_t run0, uint32_t run1, int nwin,
-                                                   uint32_t *wcnt, uint32_t *wbase,
-                                                   uint32_t *scnt) {
-  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
-  if (lane < nwin) wcnt[wid * kBallotMaxWin + lane] = run0;
-  if (lane + 32 < nwin) wcnt[wid * kBallotMaxWin + lane + 32] = run1;
-  __syncthreads();
-  if (t < nwin) {
-    uint32_t sum = 0;
-    for (int wp = 0; wp < kThreads / 32; ++wp) {
-      wbase[wp * kBallotMaxWin + t] = sum;
-      sum += wcnt[wp * kBallotMaxWin + t];
-    }
-    scnt[t] = sum;
-  }
-  __syncthreads();
-}
-
-__device__ __forceinline__ int window_bits(int nwin) {
-  int b = 0;
-  while ((1 << b) < nwin) ++b;
-  return b;
 }
 
 // Block-wide exclusive scan of scnt[0..nwin) into soff[], returns total.
@@ -172,17 +110,10 @@ __global__ void __launch_bounds__(kThreads)
   __syncthreads();
   const unsigned lt = lanemask_lt();
   const int64_t stride = static_cast<int64_t>(gridDim.x) * kThreads;
-  const bool ballot = nwin <= kBallotMaxWin;
-  const int bits = window_bits(nwin);
-  const bool two = nwin > 32;
-  const int lane = threadIdx.x & 31;
-  uint32_t run0 = 0, run1 = 0;
   auto one = [&](int32_t l, bool in_range) {
     const bool valid = in_range && static_cast<uint64_t>(static_cast<uint32_t>(l)) <
                                        static_cast<uint64_t>(n) && l >= 0;
-    const int w = valid ? (l >> log_w) : -1;
-    if (ballot) warp_rank_ballot(w, bits, two, lt, lane, run0, run1);
-    else rank_in_window(w, scnt, lt);
+    rank_in_window(valid ? (l >> log_w) : -1, scnt, lt);
   };
   if (vec) {
     const int64_t n4 = n >> 2;
@@ -213,10 +144,6 @@ __global__ void __launch_bounds__(kThreads)
       const bool ok = i < n;
       one(ok ? loc[i] : -1, ok);
     }
-  }
-  if (ballot) {
-    if (lane < nwin && run0) atomicAdd(&scnt[lane], run0);
-    if (lane + 32 < nwin && run1) atomicAdd(&scnt[lane + 32], run1);
   }
   __syncthreads();
   for (int i = threadIdx.x; i < nwin; i += kThreads)
@@ -276,14 +203,9 @@ __global__ void __launch_bounds__(kThreads)
   __shared__ uint32_t s_warp[16];
   for (int i = threadIdx.x; i < nwin; i += kThreads) scnt[i] = 0;
   __syncthreads();
-  __shared__ uint32_t wcnt[kWarpsP * kBallotMaxWin], wbase[kWarpsP * kBallotMaxWin];
   const int64_t base = static_cast<int64_t>(blockIdx.x) * kTile;
-  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  const int t = threadIdx.x;
   const unsigned lt = lanemask_lt();
-  const bool ballot = nwin <= kBallotMaxWin;
-  const int bits = window_bits(nwin);
-  const bool two = nwin > 32;
-  uint32_t run0 = 0, run1 = 0;
   int2 pr[kPer];
   int w[kPer], rank[kPer];
 #pragma unroll
@@ -307,17 +229,10 @@ __global__ void __launch_bounds__(kThreads)
       const bool valid = (i0 + q < n) && ls[q] >= 0 && static_cast<int64_t>(ls[q]) < n;
       w[e] = valid ? (ls[q] >> log_w) : -1;
       pr[e] = make_int2(ls[q], kScatter ? vs[q] : static_cast<int32_t>(i0 + q));
-      rank[e] = ballot ? warp_rank_ballot(w[e], bits, two, lt, lane, run0, run1)
-                       : rank_in_window(w[e], scnt, lt);
+      rank[e] = rank_in_window(w[e], scnt, lt);
     }
   }
   __syncthreads();
-  if (ballot) {
-    ballot_tile_counts(run0, run1, nwin, wcnt, wbase, scnt);
-#pragma unroll
-    for (int e = 0; e < kPer; ++e)
-      if (w[e] >= 0) rank[e] += static_cast<int>(wbase[wid * kBallotMaxWin + w[e]]);
-  }
   flush_runs<kPer>(pr, w, rank, nwin, log_w, scnt, soff, sgb, s_warp, stage, fill, pairs);
 }
 
@@ -334,13 +249,9 @@ __global__ void __launch_bounds__(kThreads)
   uint32_t *sgb = soff + nwin;
   __shared__ uint32_t s_warp[16];
   __shared__ int64_t s_chunk;
-  __shared__ uint32_t wcnt[kWarpsP * kBallotMaxWin], wbase[kWarpsP * kBallotMaxWin];
   const int64_t total = *total_p;
   const unsigned lt = lanemask_lt();
-  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
-  const bool ballot = nwin <= kBallotMaxWin;
-  const int bits = window_bits(nwin);
-  const bool two = nwin > 32;
+  const int t = threadIdx.x;
   while (true) {
     if (t == 0) s_chunk = static_cast<int64_t>(atomicAdd(ticket, 1ull));
     for (int i = t; i < nwin; i += kThreads) scnt[i] = 0;
@@ -365,20 +276,12 @@ __global__ void __launch_bounds__(kThreads)
       const bool valid = src[e].x >= 0;
       pr[e] = make_int2(src[e].y, valid ? ld_nc(in + src[e].x) : 0);  // {i, value}
     }
-    uint32_t run0 = 0, run1 = 0;
 #pragma unroll
     for (int e = 0; e < kPer; ++e) {
       w[e] = src[e].x >= 0 ? (pr[e].x >> log_w) : -1;
-      rank[e] = ballot ? warp_rank_ballot(w[e], bits, two, lt, lane, run0, run1)
-                       : rank_in_window(w[e], scnt, lt);
+      rank[e] = rank_in_window(w[e], scnt, lt);
     }
     __syncthreads();
-    if (ballot) {
-      ballot_tile_counts(run0, run1, nwin, wcnt, wbase, scnt);
-#pragma unroll
-      for (int e = 0; e < kPer; ++e)
-        if (w[e] >= 0) rank[e] += static_cast<int>(wbase[wid * kBallotMaxWin + w[e]]);
-    }
     flush_runs<kPer>(pr, w, rank, nwin, log_w, scnt, soff, sgb, s_warp, stage, fill2, pairs2);
     __syncthreads();
   }

@@ -102,6 +102,7 @@ struct Slot {
   size_t ws_bytes = 0;
   void *staging = nullptr;  // pinned copy of the plan tables
   size_t staging_bytes = 0;
+  uint32_t *abort_word = nullptr;  // pinned copy of the batch's abort flag
   bool busy = false;
   std::vector<std::shared_ptr<Request>> reqs;
   std::unique_ptr<edpp_batch_plan, void (*)(edpp_batch_plan *)> plan{nullptr,
@@ -152,8 +153,12 @@ void CUDART_CB on_slot_done(void *arg) {
 void retire(edpp_server *s) {
   for (int k : s->finished_slots) {
     Slot &sl = s->slots[static_cast<size_t>(k)];
+    // The host function that signalled this slot runs after every earlier
+    // operation of the stream completed; the stream itself may still count
+    // the host function as running, so "not ready" is not an error here.
     const cudaError_t e = cudaStreamQuery(sl.stream);
-    const int st = (e == cudaSuccess) ? edpp_sync_status(sl.stream, 0) : EDPP_ECUDA;
+    int st = (e == cudaSuccess || e == cudaErrorNotReady) ? EDPP_OK : EDPP_ECUDA;
+    if (st == EDPP_OK && *sl.abort_word) st = EDPP_ETIMEOUT;  // a bounded device wait expired
     const auto now = Clock::now();
     for (auto &r : sl.reqs) {
       s->alloc->release(r->off, r->req.length);
@@ -221,6 +226,10 @@ int launch_batch(edpp_server *s, int k) {
             cudaSuccess)
       return EDPP_ECUDA;
   }
+  // the batch kernel's abort flag (workspace bytes 8..11) comes back with the outputs
+  if (cudaMemcpyAsync(sl.abort_word, w + 8, sizeof(uint32_t), cudaMemcpyDeviceToHost, str) !=
+      cudaSuccess)
+    return EDPP_ECUDA;
   auto *d = new SlotDone{s, k};
   if (cudaLaunchHostFunc(str, on_slot_done, d) != cudaSuccess) {
     delete d;
@@ -332,16 +341,19 @@ int edpp_server_create(const edpp_server_config *cfg, edpp_server **out) {
                           256 * static_cast<size_t>(s->cfg.max_batch_requests) * 2 + (1 << 20);
   const size_t staging = sizeof(edpp::DevSeg) * static_cast<size_t>(s->cfg.max_batch_requests) +
                          sizeof(edpp::DevTask) * 2 * static_cast<size_t>(max_tiles);
+  const size_t staging_alloc = staging + 256;  // + the abort word
   s->slots.resize(static_cast<size_t>(cfg->slots));
   for (auto &sl : s->slots) {
     if (cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaMalloc(&sl.ws, ws_bytes) != cudaSuccess ||
-        cudaMallocHost(&sl.staging, staging) != cudaSuccess) {
+        cudaMallocHost(&sl.staging, staging_alloc) != cudaSuccess) {
       edpp_server_destroy(s.release());
       return EDPP_ENOMEM;
     }
     sl.ws_bytes = ws_bytes;
     sl.staging_bytes = staging;
+    sl.abort_word = reinterpret_cast<uint32_t *>(static_cast<char *>(sl.staging) + staging);
+    *sl.abort_word = 0;
   }
   edpp_server *raw = s.release();
   raw->thread = std::thread(scheduler, raw);
