@@ -504,7 +504,8 @@ def run_scan_workload(args, rank, world):
                          "frac_of_hbm": round(gbs / peak, 4)})
     del x24, y24
     n = 1 << args.scan_log2n
-    for dt, bpe in (("int32", 8), ("int64", 16), ("float32", 8)):
+    for dt, bpe in (() if args.scan_config1_only else
+                    (("int32", 8), ("int64", 16), ("float32", 8))):
         if dt == "int32":
             x = torch.from_numpy(edpp.gen_uniform_i32(n, 1, 0, 100)).to(dev)
         elif dt == "int64":
@@ -558,7 +559,9 @@ def run_split_workload(args, rank, world):
     ws = edpp.workspace(edpp.split_workspace_bytes(n, 4096, "soa"), dev)
     uniform = torch.from_numpy(edpp.gen_keys_uniform(n, 3)).to(dev)
     rows = []
-    for B in [2 ** k for k in range(1, 11)]:
+    blist = [int(b) for b in args.split_buckets.split(",")] if args.split_buckets else \
+        [2 ** k for k in range(1, 11)]
+    for B in blist:
         for kind in ("uniform", "zipf"):
             keys = uniform if kind == "uniform" else \
                 torch.from_numpy(edpp.gen_keys_zipf(n, 3, B, 1.0)).to(dev)
@@ -571,7 +574,7 @@ def run_split_workload(args, rank, world):
                 del keys
     if edpp.sync_status() != edpp.EDPP_OK:
         raise SystemExit("device fault in the split workload")
-    head = [r for r in rows if r["buckets"] == 256 and r["keys"] == "uniform"][0]
+    head = ([r for r in rows if r["buckets"] == 256 and r["keys"] == "uniform"] or rows)[0]
     if rank == 0:
         print(json.dumps({"metric": METRIC, "workload_metric": "stable split GB/s (16 B/pair)",
                           "value": head["GB/s"], "unit": "GB/s", "n_gpus": world,
@@ -614,6 +617,9 @@ def main(argv=None):
                     help="batch: cap on the total elements (2^30 in the config)")
     ap.add_argument("--scan-log2n", type=int, default=30)
     ap.add_argument("--split-log2n", type=int, default=28)
+    ap.add_argument("--split-buckets", default="", help="split: comma list (default 2..1024)")
+    ap.add_argument("--scan-config1-only", action="store_true",
+                    help="scan: only the config-1 rows")
     ap.add_argument("--autotune", action="store_true",
                     help="batch: run the autotuner and record its choice")
     args = ap.parse_args(argv)
