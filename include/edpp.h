@@ -212,6 +212,20 @@ int edpp_radix_sort_i32(const int32_t *keys_in, int32_t *keys_out,
                         int begin_bit, int end_bit, void *ws, size_t ws_bytes,
                         void *stream);
 
+/* ---- partitioned hash join (match count) --------------------------------- */
+
+/* Number of pairs (r, s) with r_keys[r] == s_keys[s], written to *d_count
+ * (device memory).  Both relations are split into `buckets` partitions by
+ * key & (buckets-1) (power of two <= 4096; 0 = chosen from s_len), then one
+ * block per partition pair builds a shared-memory hash table from S and
+ * probes it with R.  Counterpart of the reference's partitioned hash join,
+ * which also returns only the match count (obsolete/OpenCL/phjImpl.cpp:14-129,
+ * hj_partitioned_kernel.cl:8-107). */
+size_t edpp_hash_join_workspace_size(int64_t r_len, int64_t s_len, int buckets);
+int edpp_hash_join_count(const int32_t *r_keys, int64_t r_len, const int32_t *s_keys,
+                         int64_t s_len, int buckets, unsigned long long *d_count, void *ws,
+                         size_t ws_bytes, void *stream);
+
 /* ---- STREAM ------------------------------------------------------------- */
 
 /* copy c=a, scale c=s*a, add c=a+b, triad c=a+s*b.  Replace the kernels of

@@ -509,3 +509,42 @@ void orc_split_wi(const int32_t *in, const int32_t *vals, int64_t n, int buckets
   }
   free(his);
 }
+
+/* ---- join match count ----------------------------------------------------------
+ * The number of (r, s) pairs with equal keys, the res_len of the reference's
+ * partitioned hash join (obsolete/OpenCL/phjImpl.cpp:14-129): sort both key
+ * lists and merge runs of equal keys. */
+static int cmp_i32(const void *a, const void *b) {
+  const int32_t x = *(const int32_t *)a, y = *(const int32_t *)b;
+  return (x > y) - (x < y);
+}
+
+uint64_t orc_join_count(const int32_t *r, int64_t r_len, const int32_t *s, int64_t s_len) {
+  int32_t *a = (int32_t *)malloc(sizeof(int32_t) * (size_t)(r_len ? r_len : 1));
+  int32_t *b = (int32_t *)malloc(sizeof(int32_t) * (size_t)(s_len ? s_len : 1));
+  if (!a || !b) {
+    free(a);
+    free(b);
+    return 0;
+  }
+  memcpy(a, r, sizeof(int32_t) * (size_t)r_len);
+  memcpy(b, s, sizeof(int32_t) * (size_t)s_len);
+  qsort(a, (size_t)r_len, sizeof(int32_t), cmp_i32);
+  qsort(b, (size_t)s_len, sizeof(int32_t), cmp_i32);
+  uint64_t total = 0;
+  int64_t i = 0, j = 0;
+  while (i < r_len && j < s_len) {
+    if (a[i] < b[j]) ++i;
+    else if (a[i] > b[j]) ++j;
+    else {
+      const int32_t k = a[i];
+      int64_t ci = 0, cj = 0;
+      while (i < r_len && a[i] == k) ++i, ++ci;
+      while (j < s_len && b[j] == k) ++j, ++cj;
+      total += (uint64_t)ci * (uint64_t)cj;
+    }
+  }
+  free(a);
+  free(b);
+  return total;
+}

@@ -75,6 +75,9 @@ void orc_split_wi(const int32_t *in, const int32_t *vals, int64_t n, int buckets
 double orc_split_stable_timed(const int32_t *keys, const int32_t *vals, int64_t n, int buckets,
                               int layout, int32_t *keys_out, int32_t *vals_out);
 
+/* ---- join: number of equal-key (r, s) pairs (phjImpl.cpp:14-129 res_len) ---- */
+uint64_t orc_join_count(const int32_t *r, int64_t r_len, const int32_t *s, int64_t s_len);
+
 /* ---- measurement helpers (openmp/util/utility.cpp:23-71) ---- */
 double orc_compute_bandwidth(uint64_t num, int word_size, double ms);
 double orc_average_hampel(const double *x, int n);

@@ -36,6 +36,7 @@ _SIG = {
     "orc_split_single": (None, [_VP, _I64, _I, _I, _I, _VP]),
     "orc_split_stable_timed": (_D, [_VP, _VP, _I64, _I, _I, _VP, _VP]),
     "orc_split_wi": (None, [_VP, _VP, _I64, _I, _I, _I, _I, _VP, _VP]),
+    "orc_join_count": (ctypes.c_uint64, [_VP, _I64, _VP, _I64]),
     "orc_compute_bandwidth": (_D, [ctypes.c_uint64, _I, _D]),
     "orc_average_hampel": (_D, [_VP, _I]),
     "orc_max_threads": (_I, []),
@@ -191,6 +192,11 @@ def split_wi(keys, buckets, values=None, aos=False, local_size=256, grid_size=32
     lib().orc_split_wi(_p(keys), _p(vals), keys.shape[0], buckets, int(aos), local_size, grid_size,
                        _p(out), _p(vo))
     return out, vo
+
+
+def join_count(r, s):
+    r, s = _c(r, np.int32), _c(s, np.int32)
+    return int(lib().orc_join_count(_p(r), len(r), _p(s), len(s)))
 
 
 def average_hampel(x):

@@ -51,3 +51,14 @@ def test_soa_stability(orc, edpp):
         v = vo[b == bb]
         assert np.all(np.diff(v) > 0)
     np.testing.assert_array_equal(keys[vo], ko)
+
+
+@pytest.mark.parametrize("r_len,s_len,hi", [(0, 5, 3), (5, 0, 3), (1, 1, 0), (1000, 700, 50),
+                                            (3000, 4000, 100000)])
+def test_join_count_equals_pair_count(orc, edpp, r_len, s_len, hi):
+    # the join oracle (sort-merge) against the definition: sum over keys of
+    # count_R(key) * count_S(key), here by brute-force pair comparison
+    r = edpp.gen_uniform_i32(r_len, 11, -hi, hi)
+    s = edpp.gen_uniform_i32(s_len, 12, -hi, hi)
+    want = int((r[:, None] == s[None, :]).sum()) if r_len and s_len else 0
+    assert orc.join_count(r, s) == want
