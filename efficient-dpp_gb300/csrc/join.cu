@@ -89,6 +89,73 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// ---- non-partitioned form: one table in HBM/L2 -------------------------------
+// (obsolete/OpenCL/nphjImpl.cpp:15-144, hj_non_partitioned_kernel.cl:9-77):
+// build a table of 2^bits >= 2*|build side| slots, then every probe tuple walks
+// its chain.  Same {count, key} slots as the shared-memory table; a 129 MB L2
+// holds the table for build sides up to about 4M tuples.
+__device__ __forceinline__ uint32_t np_slot(uint32_t key, int bits) {
+  return (key * 0x9E3779B1u) >> (32 - bits);
+}
+
+__global__ void __launch_bounds__(256)
+    join_np_build_kernel(const int32_t *__restrict__ keys, int64_t n,
+                         unsigned long long *__restrict__ table, int bits) {
+  const uint32_t mask = (1u << bits) - 1u;
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const uint32_t key = static_cast<uint32_t>(keys[i]);
+    const unsigned long long entry = (1ull << 32) | key;
+    uint32_t h = np_slot(key, bits);
+    while (true) {
+      const unsigned long long cur = atomicCAS(&table[h], 0ull, entry);
+      if (cur == 0ull) break;
+      if (static_cast<uint32_t>(cur) == key) {
+        atomicAdd(&table[h], 1ull << 32);
+        break;
+      }
+      h = (h + 1) & mask;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    join_np_probe_kernel(const int32_t *__restrict__ keys, int64_t n,
+                         const unsigned long long *__restrict__ table, int bits,
+                         unsigned long long *__restrict__ count) {
+  __shared__ unsigned long long s_red[8];
+  const uint32_t mask = (1u << bits) - 1u;
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  unsigned long long matches = 0;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const uint32_t key = static_cast<uint32_t>(__ldg(keys + i));
+    uint32_t h = np_slot(key, bits);
+    unsigned long long e;
+    while ((e = __ldg(table + h)) != 0ull) {
+      if (static_cast<uint32_t>(e) == key) {
+        matches += e >> 32;
+        break;
+      }
+      h = (h + 1) & mask;
+    }
+  }
+#pragma unroll
+  for (int m = 16; m >= 1; m >>= 1) matches += __shfl_xor_sync(0xffffffffu, matches, m);
+  if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = matches;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long t = 0;
+    for (int w = 0; w < 8; ++w) t += s_red[w];
+    if (t) atomicAdd(count, t);
+  }
+}
+
+int np_bits(int64_t build_len) {
+  int bits = 1;
+  while ((int64_t{1} << bits) < 2 * build_len) ++bits;  // load factor <= 0.5
+  return bits;
+}
+
 int auto_buckets(int64_t s_len) {
   int b = 1;
   while (b < 4096 && s_len / b > kChunk / 2) b *= 2;  // a partition fills about half a build
@@ -169,6 +236,37 @@ int edpp_hash_join_count(const int32_t *r_keys, int64_t r_len, const int32_t *s_
   if (attr[dev] != cudaSuccess) return EDPP_ECUDA;
   join_probe_kernel<<<static_cast<unsigned>(buckets), kThreads, kTable * sizeof(unsigned long long),
                       st>>>(rp, r_len, rs, sp, s_len, ss, buckets, d_count);
+  return launch_status();
+}
+
+size_t edpp_hash_join_np_workspace_size(int64_t build_len) {
+  if (build_len < 0 || build_len > INT32_MAX) return 0;
+  return (size_t{1} << edpp::np_bits(edpp::max64(build_len, 1))) * sizeof(unsigned long long);
+}
+
+int edpp_hash_join_np_count(const int32_t *build_keys, int64_t build_len, const int32_t *probe_keys,
+                            int64_t probe_len, unsigned long long *d_count, void *ws,
+                            size_t ws_bytes, void *stream) {
+  using namespace edpp;
+  if (build_len < 0 || probe_len < 0 || build_len > INT32_MAX || probe_len > INT32_MAX || !d_count)
+    return EDPP_EINVAL;
+  cudaStream_t st = as_stream(stream);
+  if (cudaMemsetAsync(d_count, 0, sizeof(unsigned long long), st) != cudaSuccess) return EDPP_ECUDA;
+  if (build_len == 0 || probe_len == 0) return EDPP_OK;
+  if (!build_keys || !probe_keys) return EDPP_EINVAL;
+  const int bits = np_bits(build_len);
+  const size_t bytes = (size_t{1} << bits) * sizeof(unsigned long long);
+  if (!ws || ws_bytes < bytes || !aligned16(ws)) return EDPP_ENOMEM;
+  auto *table = static_cast<unsigned long long *>(ws);
+  if (cudaMemsetAsync(table, 0, bytes, st) != cudaSuccess) return EDPP_ECUDA;
+  const int sms = device_sm_count();
+  const int64_t cap = static_cast<int64_t>(sms) * 8;  // 8 resident blocks of 256 per SM
+  const unsigned gb = static_cast<unsigned>(std::max<int64_t>(1, std::min(cap, (build_len + 255) / 256)));
+  join_np_build_kernel<<<gb, 256, 0, st>>>(build_keys, build_len, table, bits);
+  int s = launch_status();
+  if (s != EDPP_OK) return s;
+  const unsigned gp = static_cast<unsigned>(std::max<int64_t>(1, std::min(cap, (probe_len + 255) / 256)));
+  join_np_probe_kernel<<<gp, 256, 0, st>>>(probe_keys, probe_len, table, bits, d_count);
   return launch_status();
 }
 

@@ -61,6 +61,8 @@ SIGNATURES = {
     "edpp_radix_sort_i32": (_I, [_VP, _VP, _VP, _VP, _I64, _I, _I, _VP, _SZ, _VP]),
     "edpp_hash_join_workspace_size": (_SZ, [_I64, _I64, _I]),
     "edpp_hash_join_count": (_I, [_VP, _I64, _VP, _I64, _I, _VP, _VP, _SZ, _VP]),
+    "edpp_hash_join_np_workspace_size": (_SZ, [_I64]),
+    "edpp_hash_join_np_count": (_I, [_VP, _I64, _VP, _I64, _VP, _VP, _SZ, _VP]),
     "edpp_stream_copy_f32": (_I, [_VP, _VP, _I64, _VP]),
     "edpp_stream_scale_f32": (_I, [_VP, _VP, _F, _I64, _VP]),
     "edpp_stream_add_f32": (_I, [_VP, _VP, _VP, _I64, _VP]),
@@ -319,19 +321,30 @@ def radix_sort(keys, values=None, begin_bit=0, end_bit=32, keys_out=None, values
     return keys_out, values_out
 
 
-def hash_join_count(r_keys, s_keys, buckets: int = 0, ws=None) -> int:
-    """Number of equal-key pairs between R and S (partitioned hash join)."""
+def hash_join_count(r_keys, s_keys, buckets: int = 0, ws=None, partitioned: bool = True,
+                    count=None) -> int:
+    """Number of equal-key pairs between R and S.  partitioned=True: split
+    both sides, one shared-memory table per partition; False: one table in
+    device memory built from S and probed with R.  With `count` (a 1-element
+    int64 CUDA tensor) the result stays on the device and None is returned."""
     torch = _torch()
     _cuda_tensor(r_keys, torch.int32, "r_keys")
     _cuda_tensor(s_keys, torch.int32, "s_keys")
-    cnt = torch.zeros(1, dtype=torch.int64, device=r_keys.device)
-    if ws is None:
-        ws = workspace(lib().edpp_hash_join_workspace_size(r_keys.numel(), s_keys.numel(),
-                                                           int(buckets)), r_keys.device)
-    check(lib().edpp_hash_join_count(_p(r_keys), r_keys.numel(), _p(s_keys), s_keys.numel(),
-                                     int(buckets), _p(cnt), _p(ws), ws.numel(),
-                                     current_stream_handle()), "hash_join_count")
-    return int(cnt.item())
+    cnt = count if count is not None else torch.zeros(1, dtype=torch.int64, device=r_keys.device)
+    st = current_stream_handle()
+    if partitioned:
+        if ws is None:
+            ws = workspace(lib().edpp_hash_join_workspace_size(r_keys.numel(), s_keys.numel(),
+                                                               int(buckets)), r_keys.device)
+        check(lib().edpp_hash_join_count(_p(r_keys), r_keys.numel(), _p(s_keys), s_keys.numel(),
+                                         int(buckets), _p(cnt), _p(ws), ws.numel(), st),
+              "hash_join_count")
+    else:
+        if ws is None:
+            ws = workspace(lib().edpp_hash_join_np_workspace_size(s_keys.numel()), r_keys.device)
+        check(lib().edpp_hash_join_np_count(_p(s_keys), s_keys.numel(), _p(r_keys), r_keys.numel(),
+                                            _p(cnt), _p(ws), ws.numel(), st), "hash_join_np_count")
+    return None if count is not None else int(cnt.item())
 
 
 def stream(op: str, a, b=None, scalar=3, out=None):

@@ -226,6 +226,16 @@ int edpp_hash_join_count(const int32_t *r_keys, int64_t r_len, const int32_t *s_
                          int64_t s_len, int buckets, unsigned long long *d_count, void *ws,
                          size_t ws_bytes, void *stream);
 
+/* Non-partitioned form: one open-addressing table of 2^k >= 2*build_len
+ * slots (8 bytes each) in the workspace, built from build_keys and probed
+ * with probe_keys; same count.  Counterpart of the reference's
+ * non-partitioned hash join (obsolete/OpenCL/nphjImpl.cpp:15-144,
+ * hj_non_partitioned_kernel.cl:9-77). */
+size_t edpp_hash_join_np_workspace_size(int64_t build_len);
+int edpp_hash_join_np_count(const int32_t *build_keys, int64_t build_len,
+                            const int32_t *probe_keys, int64_t probe_len,
+                            unsigned long long *d_count, void *ws, size_t ws_bytes, void *stream);
+
 /* ---- STREAM ------------------------------------------------------------- */
 
 /* copy c=a, scale c=s*a, add c=a+b, triad c=a+s*b.  Replace the kernels of
