@@ -63,6 +63,10 @@ SIGNATURES = {
     "edpp_hash_join_count": (_I, [_VP, _I64, _VP, _I64, _I, _VP, _VP, _SZ, _VP]),
     "edpp_hash_join_np_workspace_size": (_SZ, [_I64]),
     "edpp_hash_join_np_count": (_I, [_VP, _I64, _VP, _I64, _VP, _VP, _SZ, _VP]),
+    "edpp_access_scale_i32": (_I, [_VP, _VP, _I, _I, _I, _I, _VP]),
+    "edpp_access_wg_i32": (_I, [_VP, _I64, _VP, _I, _I, _VP, _VP, _VP]),
+    "edpp_cache_heat_i32": (_I, [_VP, _I64, _I, _I, _VP]),
+    "edpp_local_scan_i32": (_I, [_VP, _VP, _I, _I, _I, _VP]),
     "edpp_stream_copy_f32": (_I, [_VP, _VP, _I64, _VP]),
     "edpp_stream_scale_f32": (_I, [_VP, _VP, _F, _I64, _VP]),
     "edpp_stream_add_f32": (_I, [_VP, _VP, _VP, _I64, _VP]),
@@ -345,6 +349,59 @@ def hash_join_count(r_keys, s_keys, buckets: int = 0, ws=None, partitioned: bool
         check(lib().edpp_hash_join_np_count(_p(s_keys), s_keys.numel(), _p(r_keys), r_keys.numel(),
                                             _p(cnt), _p(ws), ws.numel(), st), "hash_join_np_count")
     return None if count is not None else int(cnt.item())
+
+
+ACCESS_PATTERNS = {"column": 0, "row": 1, "mixed": 2, "vec": 3}
+LOCAL_SCAN_SCHEMES = {"lm": 0, "reg": 1, "lm_reg": 2, "warp": 3}
+
+
+def access_scale(inp, out, repeat: int, pattern: str, local_size: int = 512,
+                 grid_size: int = 32768):
+    """out[i] = 3*in[i] for i < local_size*grid_size*repeat, with the given
+    thread-to-element map."""
+    torch = _torch()
+    _cuda_tensor(inp, torch.int32, "in")
+    _cuda_tensor(out, torch.int32, "out")
+    n = local_size * grid_size * repeat
+    if inp.numel() < n or out.numel() < n:
+        raise ValueError("buffers hold fewer than local_size*grid_size*repeat elements")
+    check(lib().edpp_access_scale_i32(_p(inp), _p(out), repeat, ACCESS_PATTERNS[pattern],
+                                      local_size, grid_size, current_stream_handle()),
+          "access_scale")
+
+
+def access_wg(inp, order, local_size: int = 1, out=None, ticket=None):
+    """Block-order sweep: per-chunk sums of the low bits, chunk visit order
+    `order` (int32 CUDA tensor of grid_size chunk ids)."""
+    torch = _torch()
+    _cuda_tensor(inp, torch.int32, "in")
+    _cuda_tensor(order, torch.int32, "order")
+    g = order.numel()
+    out = out if out is not None else torch.zeros(g, dtype=torch.int64, device=inp.device)
+    ticket = ticket if ticket is not None else torch.zeros(1, dtype=torch.int32, device=inp.device)
+    check(lib().edpp_access_wg_i32(_p(inp), inp.numel(), _p(order), g, local_size, _p(ticket),
+                                   _p(out), current_stream_handle()), "access_wg")
+    return out
+
+
+def cache_heat(data, local_size: int = 512, grid_size: int = 32768):
+    torch = _torch()
+    _cuda_tensor(data, torch.int32, "data")
+    check(lib().edpp_cache_heat_i32(_p(data), data.numel(), local_size, grid_size,
+                                    current_stream_handle()), "cache_heat")
+
+
+def local_scan(inp, tile_size: int, scheme: str, repeat: int = 1, out=None):
+    """Exclusive scan of the first 512*tile_size elements by one block."""
+    torch = _torch()
+    _cuda_tensor(inp, torch.int32, "in")
+    n = 512 * tile_size
+    if inp.numel() < n:
+        raise ValueError("input holds fewer than 512*tile_size elements")
+    out = out if out is not None else torch.empty(n, dtype=torch.int32, device=inp.device)
+    check(lib().edpp_local_scan_i32(_p(inp), _p(out), tile_size, LOCAL_SCAN_SCHEMES[scheme],
+                                    repeat, current_stream_handle()), "local_scan")
+    return out
 
 
 def stream(op: str, a, b=None, scalar=3, out=None):

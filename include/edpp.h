@@ -236,6 +236,43 @@ int edpp_hash_join_np_count(const int32_t *build_keys, int64_t build_len,
                             const int32_t *probe_keys, int64_t probe_len,
                             unsigned long long *d_count, void *ws, size_t ws_bytes, void *stream);
 
+/* ---- access-pattern and single-block scan microbenchmarks --------------- */
+
+/* Scale out[i] = 3 * in[i] over i in [0, local_size*grid_size*repeat) with
+ * the reference's three thread-to-element maps (opencl/kernels/mem_kernel.cl:
+ * 33-69, driven by opencl/test/test_access.cpp): COLUMN, thread g touches
+ * g + k*G; ROW, g*repeat + k; MIXED, warp-contiguous chunks with lanes
+ * stepping by 32.  VEC is the 16-byte grid-stride form the STREAM kernels use
+ * (local_size/grid_size only set the element count). */
+typedef enum {
+  EDPP_ACCESS_COLUMN = 0,
+  EDPP_ACCESS_ROW = 1,
+  EDPP_ACCESS_MIXED = 2,
+  EDPP_ACCESS_VEC = 3
+} edpp_access_pattern;
+int edpp_access_scale_i32(const int32_t *in, int32_t *out, int repeat, int pattern,
+                          int local_size, int grid_size, void *stream);
+/* Block-order sweep (mem_kernel.cl:71-87, opencl/test/test_access_wg.cpp):
+ * grid_size blocks of local_size threads; the block holding ticket t sums
+ * the low bits of chunk order[t] (len / grid_size elements) into out[order[t]].
+ * *ticket (device word) is zeroed on the stream first. */
+int edpp_access_wg_i32(const int32_t *in, int64_t len, const int32_t *order, int grid_size,
+                       int local_size, unsigned *ticket, long long *out, void *stream);
+/* Write-only warm-up data[c] = c in warp-contiguous chunks (mem_kernel.cl:89-107). */
+int edpp_cache_heat_i32(int32_t *data, int64_t length, int local_size, int grid_size,
+                        void *stream);
+/* Exclusive scan of 512*tile_size int32 by one block of 512 threads, launched
+ * `repeat` times (opencl/kernels/scan_local_kernel.cl:530-695, driven by
+ * opencl/test/test_scan_local.cpp).  tile_size 1..49; in != out. */
+typedef enum {
+  EDPP_LOCAL_SCAN_LM = 0,     /* tile in shared memory, serial row scans */
+  EDPP_LOCAL_SCAN_REG = 1,    /* rows loaded straight into registers */
+  EDPP_LOCAL_SCAN_LM_REG = 2, /* coalesced via shared memory, rows in registers */
+  EDPP_LOCAL_SCAN_WARP = 3    /* LM_REG with a warp-shuffle block scan */
+} edpp_local_scan_scheme;
+int edpp_local_scan_i32(const int32_t *in, int32_t *out, int tile_size, int scheme, int repeat,
+                        void *stream);
+
 /* ---- STREAM ------------------------------------------------------------- */
 
 /* copy c=a, scale c=s*a, add c=a+b, triad c=a+s*b.  Replace the kernels of
