@@ -588,6 +588,135 @@ def run_split_workload(args, rank, world):
     return 0
 
 
+def run_join_workload(args, rank, world):
+    """Hash join match count, partitioned (split both sides, shared-memory
+    table per partition) and non-partitioned (one device table), |R| = 2^k
+    keys and |S| in {2^k, 2^(k-4)}, uniform over [0, 2^k) (seeds 7, 8)."""
+    import torch
+
+    import edpp
+    edpp.lib()
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.set_device(dev)
+    peak, peak_kind = measured_peak_gbs()
+    k = args.join_log2n
+    rows = []
+    r = torch.from_numpy(edpp.gen_uniform_i32(1 << k, 7, 0, (1 << k) - 1)).to(dev)
+    cnt = torch.zeros(1, dtype=torch.int64, device=dev)
+    for s_log2 in (k, k - 4):
+        s = torch.from_numpy(edpp.gen_uniform_i32(1 << s_log2, 8, 0, (1 << k) - 1)).to(dev)
+        for part in (True, False):
+            nbytes = (edpp.lib().edpp_hash_join_workspace_size(r.numel(), s.numel(), 0) if part
+                      else edpp.lib().edpp_hash_join_np_workspace_size(s.numel()))
+            ws = edpp.workspace(nbytes, dev)
+            ms = _event_ms(lambda: edpp.hash_join_count(r, s, ws=ws, partitioned=part, count=cnt),
+                           args.steps, args.warmup)
+            tuples = r.numel() + s.numel()
+            rows.append({"r": r.numel(), "s": s.numel(),
+                         "form": "partitioned" if part else "non-partitioned",
+                         "ms": round(ms, 4), "Mtuples/s": round(tuples / (ms * 1e-3) / 1e6, 1),
+                         "matches": int(cnt.item())})
+            del ws
+        del s
+    if edpp.sync_status() != edpp.EDPP_OK:
+        raise SystemExit("device fault in the join workload")
+    head = max(rows, key=lambda x: x["Mtuples/s"] if x["s"] == x["r"] else 0)
+    if rank == 0:
+        print(json.dumps({"metric": METRIC, "workload_metric": "join Mtuples/s ((|R|+|S|)/t)",
+                          "value": head["Mtuples/s"], "unit": "Mtuples/s", "n_gpus": world,
+                          "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["ms"],
+                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                          "dtype": "int32", "data": "synthetic", "peak": peak,
+                          "peak_source": peak_kind,
+                          "config": {"workload": f"hash join count, |R|=2^{k}, |S|=2^{k} and "
+                                                 f"2^{k - 4}, keys uniform [0,2^{k})"},
+                          "rows": rows}), flush=True)
+    return 0
+
+
+def run_access_workload(args, rank, world):
+    """Access-pattern sweeps: scale with column / row / mixed / vector maps
+    (local 512, grid 32768, repeat 1..20 as the reference's access test),
+    block-order sweep (chunks 8 KB..8 MB, interleaved or shuffled order,
+    cold or after a cache-heat pass), single-block matrix scans (tiles 1..49)."""
+    import numpy as np
+    import torch
+
+    import edpp
+    edpp.lib()
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.set_device(dev)
+    peak, peak_kind = measured_peak_gbs()
+    local, grid = 512, 32768
+    repeats = [1, 2, 4, 8, 12, 16, 20]
+    nmax = local * grid * max(repeats)
+    a = torch.arange(nmax, dtype=torch.int32, device=dev)
+    b = torch.empty_like(a)
+    scale = []
+    for pattern in ("column", "row", "mixed", "vec"):
+        for rep in repeats:
+            ms = _event_ms(lambda: edpp.access_scale(a, b, rep, pattern, local, grid),
+                           args.steps, args.warmup)
+            gbs = 8 * local * grid * rep / (ms * 1e-3) / 1e9
+            scale.append({"pattern": pattern, "repeat": rep, "ms": round(ms, 4),
+                          "GB/s": round(gbs, 1), "frac_of_hbm": round(gbs / peak, 4)})
+    del b
+    length = 1 << args.access_wg_log2n
+    data = a[:length]
+    wg = []
+    for order_kind in ("interleaved", "random"):
+        for loaded in (False, True):
+            for kb in (8192, 1024, 128, 8):
+                g = length * 4 // (kb * 1024)
+                order = np.arange(g, dtype=np.int32)
+                if order_kind == "random":
+                    order = np.random.default_rng(9).permutation(g).astype(np.int32)
+                d_order = torch.from_numpy(order).to(dev)
+                out = torch.zeros(g, dtype=torch.int64, device=dev)
+                tick = torch.zeros(1, dtype=torch.int32, device=dev)
+                for lsz in (1, 256):
+                    # "loaded": the input was just written by the heat pass
+                    pre = (lambda: edpp.cache_heat(data, 512, 32768)) if loaded else None
+
+                    def call():
+                        if pre is not None:
+                            pre()
+                        edpp.access_wg(data, d_order, lsz, out=out, ticket=tick)
+                    if loaded:
+                        # time the sweep alone, after the heat pass
+                        ms_h = _event_ms(pre, 2, 1)
+                        ms = _event_ms(call, 2, 1) - ms_h
+                    else:
+                        ms = _event_ms(call, 2, 1)
+                    wg.append({"order": order_kind, "loaded": loaded, "chunk_kb": kb,
+                               "blocks": g, "threads": lsz, "ms": round(ms, 4),
+                               "GB/s": round(4 * length / (max(ms, 1e-6) * 1e-3) / 1e9, 1)})
+    del a
+    lscan = []
+    src = torch.from_numpy(edpp.gen_uniform_i32(512 * 49, 7, 0, 15)).to(dev)
+    dst = torch.empty_like(src)
+    for scheme in ("lm", "reg", "lm_reg", "warp"):
+        for tile in (1, 2, 4, 8, 16, 24, 32, 49):
+            reps = 200
+            ms = _event_ms(lambda: edpp.local_scan(src, tile, scheme, repeat=reps, out=dst), 2, 1)
+            lscan.append({"scheme": scheme, "tile": tile, "us_per_launch": round(ms * 1e3 / reps, 2)})
+    if edpp.sync_status() != edpp.EDPP_OK:
+        raise SystemExit("device fault in the access workload")
+    head = max(scale, key=lambda x: x["GB/s"])
+    if rank == 0:
+        print(json.dumps({"metric": METRIC, "workload_metric": "scale GB/s (8 B/elem), best map",
+                          "value": head["GB/s"], "unit": "GB/s", "n_gpus": world,
+                          "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["ms"],
+                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                          "dtype": "int32", "data": "synthetic", "peak": peak,
+                          "peak_source": peak_kind,
+                          "config": {"workload": "access-pattern sweeps (scale 512x32768xR, "
+                                                 f"block-order 2^{args.access_wg_log2n}, "
+                                                 "matrix scans 512xT)"},
+                          "scale": scale, "block_order": wg, "local_scan": lscan}), flush=True)
+    return 0
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawTextHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -604,7 +733,7 @@ def main(argv=None):
     ap.add_argument("--no-compare", action="store_true",
                     help="skip timing the other gather/scatter schedule")
     ap.add_argument("--workload", default="gs_stream",
-                    choices=["gs_stream", "batch", "serve", "scan", "split"],
+                    choices=["gs_stream", "batch", "serve", "scan", "split", "join", "access"],
                     help="gs_stream: multi-pass gather/scatter + STREAM (default); "
                          "batch: 4096 uneven segments, batched vs plain; "
                          "serve: Poisson request stream through the server")
@@ -618,6 +747,8 @@ def main(argv=None):
     ap.add_argument("--scan-log2n", type=int, default=30)
     ap.add_argument("--split-log2n", type=int, default=28)
     ap.add_argument("--split-buckets", default="", help="split: comma list (default 2..1024)")
+    ap.add_argument("--join-log2n", type=int, default=26)
+    ap.add_argument("--access-wg-log2n", type=int, default=26)
     ap.add_argument("--scan-config1-only", action="store_true",
                     help="scan: only the config-1 rows")
     ap.add_argument("--autotune", action="store_true",
@@ -636,6 +767,10 @@ def main(argv=None):
         return run_scan_workload(args, rank, world)
     if args.workload == "split":
         return run_split_workload(args, rank, world)
+    if args.workload == "join":
+        return run_join_workload(args, rank, world)
+    if args.workload == "access":
+        return run_access_workload(args, rank, world)
 
     import numpy as np
     import torch
