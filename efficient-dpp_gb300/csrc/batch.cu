@@ -126,17 +126,22 @@ __global__ void __launch_bounds__(kThreads, 3)
   __syncthreads();
   uint32_t phase = 0;
   const unsigned lt = lanemask_lt_b();
-  // Thread 0 keeps the next ticket in hand while the block works on the
-  // current task, hiding the atomic's latency.  A block's current task never
-  // waits on its own prefetched task (waits only target earlier tickets),
-  // and tickets are handed out in order, so progress is unaffected.
-  int next_task = 0;
-  if (t == 0) next_task = static_cast<int>(atomicAdd(ticket, 1ull));
+  // Thread 0 takes the next ticket early, once nothing can wait on the
+  // current task any more: a SCAN tile after publishing its prefix, a SPLIT
+  // tile once its histogram is ready, a GATHER tile at once (HIST tiles take
+  // it at the loop top).  The atomic's latency then hides behind the rest of
+  // the task, and a block never holds an unstarted task while the current one
+  // can still make others wait, so waits do not chain.
+  int next_task = -1;
+  auto take_next = [&]() {
+    if (t == 0 && next_task < 0) next_task = static_cast<int>(atomicAdd(ticket, 1ull));
+  };
 
   while (true) {
     if (t == 0) {
+      take_next();
       s_task = next_task;
-      if (next_task < num_tasks) next_task = static_cast<int>(atomicAdd(ticket, 1ull));
+      next_task = -1;
     }
     __syncthreads();
     const int task_id = s_task;
@@ -175,11 +180,13 @@ __global__ void __launch_bounds__(kThreads, 3)
         }
         if (lane == 0) sm.scan.sh.prefix = ok ? prefix : 0;
       }
+      take_next();
       __syncthreads();
       TS32::phase3<false>(c, wex, sm.scan.sh, sm.scan.sh.prefix);
       TS32::store(out0, gbase, count, c, (reinterpret_cast<uintptr_t>(out0 + gbase) & 15) == 0);
     } else if (task.kind == kTaskGather) {
       // ---- permutation gather tile, indices local to the segment ----
+      take_next();
       const int32_t *src = in0 + seg.off;
       constexpr int kPerT = kTile / kThreads;  // 16: every load in flight at once
       int v[kPerT], idx[kPerT];
@@ -243,6 +250,7 @@ __global__ void __launch_bounds__(kThreads, 3)
           atomicOr(abort_flag, 1u);
         }
         s_flag = ok ? 1 : 0;
+        take_next();
       }
       __syncthreads();
       if (s_flag) {
@@ -491,19 +499,24 @@ int edpp_batch_launch(const edpp_batch_plan *plan, const int32_t *in0, const int
   if (cudaMemsetAsync(w + p.off_ctrl, 0, p.off_state - p.off_ctrl + p.scan_state_bytes, st) !=
       cudaSuccess)
     return EDPP_ECUDA;
-  const int sms = device_sm_count();
-  int64_t blocks = static_cast<int64_t>(sms) * p.blocks_per_sm;
-  blocks = min64(blocks, static_cast<int64_t>(p.tasks.size()));
   static std::once_flag attr_once[64];
   static cudaError_t attr_err[64];
+  static int resident[64];
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64) dev = 0;
   std::call_once(attr_once[dev], [dev] {
     attr_err[dev] = cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(sizeof(BatchSmem)));
+    if (attr_err[dev] == cudaSuccess)
+      attr_err[dev] = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident[dev], batch_kernel,
+                                                                    kThreads, sizeof(BatchSmem));
   });
   if (attr_err[dev] != cudaSuccess) return EDPP_ECUDA;
+  // blocks beyond what stays resident would only start once the queue is empty
+  const int per_sm = std::max(1, std::min(p.blocks_per_sm, resident[dev]));
+  int64_t blocks = static_cast<int64_t>(device_sm_count()) * per_sm;
+  blocks = min64(blocks, static_cast<int64_t>(p.tasks.size()));
   batch_kernel<<<static_cast<unsigned>(max64(blocks, 1)), kThreads, sizeof(BatchSmem), st>>>(
       reinterpret_cast<const DevSeg *>(w + p.off_segs),
       reinterpret_cast<const DevTask *>(w + p.off_tasks), static_cast<int>(p.tasks.size()), in0,
@@ -574,7 +587,7 @@ extern "C" int edpp_batch_autotune(const edpp_segment *segs, int num_segs, const
   }
   float best_t = 1e30f;
   int status = EDPP_OK;
-  for (int bps : {2, 3, 4, 6, 8}) {
+  for (int bps : {1, 2, 3}) {  // the launch clamps to the resident count (3)
     for (int defer : {0, 1, 2, 4}) {
       for (int lf : {0, 1}) {
         edpp_batch_tuning tu{bps, defer, lf, 0};

@@ -128,28 +128,23 @@ __global__ void __launch_bounds__(kThreads)
   int64_t cur = s_next;
   int slot = 0;
   uint32_t phase = 0;  // bit s: parity of the next completion of bar[s]
-  uint32_t bulk_cur = 0, bulk_nxt = 0;
+  uint32_t bulk_cur = 0;
   if (cur < num_tiles)
     bulk_cur = stage_tile<T, kTile, kThreads>(buf[0], in + cur * kTile, count_of(cur), tma, &bar[0]);
-  bool stop = false;
   while (cur < num_tiles) {
-    __syncthreads();  // previous tile done: buf[slot^1] and sh are free, s_next consumed
-    if (threadIdx.x == 0) s_next = static_cast<int64_t>(atomicAdd(ticket, 1ull)) + ticket_base;
-    __syncthreads();
-    const int64_t nxt = s_next;
-    bulk_nxt = 0;
-    if (nxt < num_tiles)
-      bulk_nxt = stage_tile<T, kTile, kThreads>(buf[slot ^ 1], in + nxt * kTile, count_of(nxt), tma,
-                                                &bar[slot ^ 1]);
+    // The next ticket is taken only once this tile's inclusive prefix is
+    // published: a block never holds an unstarted tile while it waits in a
+    // look-back, so no tile waits behind another block's wait (holding it
+    // earlier chains the waits and serialises the whole scan).  Its bulk
+    // copy then overlaps this tile's output phase.
     const int count = count_of(cur);
     bool failed = false;
     if (bulk_cur) {
       failed = !mbar_wait_bounded(&bar[slot], (phase >> slot) & 1u, timeout_ns, fault);
       phase ^= 1u << slot;
     }
-    if (__syncthreads_or(failed)) {
+    if (__syncthreads_or(failed)) {  // also: sh and s_next of the last tile are consumed
       atomicOr(abort_flag, 1u);
-      stop = true;
       break;
     }
     Chunk<T> c[kChunks];
@@ -166,22 +161,24 @@ __global__ void __launch_bounds__(kThreads)
       } else {
         prefix = lookback_warp<T>(st, cur, agg, lane, timeout_ns, fault, abort_flag, ok);
       }
-      if (lane == 0) sh.prefix = ok ? prefix : zero_of<T>();
+      if (lane == 0) {
+        sh.prefix = ok ? prefix : zero_of<T>();
+        s_next = static_cast<int64_t>(atomicAdd(ticket, 1ull)) + ticket_base;
+      }
     }
     __syncthreads();
-    if (fault_raised(abort_flag)) {  // a failed call writes nothing further
-      stop = true;
-      break;
-    }
+    if (fault_raised(abort_flag)) break;  // a failed call writes nothing further
+    const int64_t nxt = s_next;
+    uint32_t bulk_nxt = 0;
+    if (nxt < num_tiles)  // buf[slot ^ 1] was consumed by the previous tile's phase 1
+      bulk_nxt = stage_tile<T, kTile, kThreads>(buf[slot ^ 1], in + nxt * kTile, count_of(nxt), tma,
+                                                &bar[slot ^ 1]);
     S::template phase3<kInclusive>(c, wex, sh, sh.prefix);
     S::store(out, cur * kTile, count, c, vec_out);
     cur = nxt;
     bulk_cur = bulk_nxt;
     slot ^= 1;
   }
-  // Leaving early: let the prefetched tile's bulk copy land before the
-  // block's shared memory is released (bounded).
-  if (stop && bulk_nxt) mbar_wait_bounded(&bar[slot ^ 1], (phase >> (slot ^ 1)) & 1u, timeout_ns, fault);
 }
 
 // ---- RTS / SSA building blocks ----------------------------------------------
