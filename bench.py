@@ -68,6 +68,8 @@ def call_launches(name, p, method="partition"):
     """Kernels of this library one call launches."""
     if name not in ("gather", "scatter"):
         return 1
+    if method == "tiled":  # count, scan, partition, refine, (fetch, refine,) apply
+        return 7 if name == "gather" else 5
     if method == "sweep" or p == 1:
         return p
     return 5 if name == "gather" else 4  # count, bases, partition, (fetch,) apply
@@ -728,7 +730,7 @@ def main(argv=None):
     ap.add_argument("--cpu-sample", type=int, default=1 << 26)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--method", default="partition", choices=["partition", "sweep"],
+    ap.add_argument("--method", default="partition", choices=["partition", "sweep", "tiled"],
                     help="gather/scatter schedule of the timed step")
     ap.add_argument("--no-compare", action="store_true",
                     help="skip timing the other gather/scatter schedule")
@@ -793,8 +795,8 @@ def main(argv=None):
     d_out = torch.empty(n, dtype=torch.int32, device=dev)
     d_fout = torch.empty(n, dtype=torch.float32, device=dev)
     # one workspace serves every pass count (allocated outside the timed region)
-    ws = edpp.workspace(max(edpp.gs_workspace_bytes(k, n, p) for k in ("gather", "scatter")
-                            for p in PASSES), dev)
+    ws = edpp.workspace(max(edpp.gs_workspace_bytes(k, n, p, m) for k in ("gather", "scatter")
+                            for p in PASSES for m in ("partition", "tiled")), dev)
 
     def run_call(name, p, method=args.method):
         if name == "gather":
@@ -872,22 +874,26 @@ def main(argv=None):
     # ---- the other schedule, per call, for comparison (not in `value`) ------
     compare = None
     if not args.no_compare:
-        other = "sweep" if args.method == "partition" else "partition"
-        compare = {"method": other}
-        for c in calls:
-            if c[0] not in ("gather", "scatter"):
+        compare = {}
+        for other in ("sweep", "partition", "tiled"):
+            if other == args.method:
                 continue
-            run_call(*c, method=other)
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            for _ in range(args.steps):
+            cm = {}
+            for c in calls:
+                if c[0] not in ("gather", "scatter"):
+                    continue
                 run_call(*c, method=other)
-            e1.record(stream)
-            torch.cuda.synchronize()
-            ms = e0.elapsed_time(e1) / args.steps
-            compare[f"{c[0]}_p{c[1]}"] = {"ms": round(ms, 4),
-                                          "GB/s": round(call_bytes(c[0], n) / (ms * 1e-3) / 1e9, 1)}
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                for _ in range(args.steps):
+                    run_call(*c, method=other)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ms = e0.elapsed_time(e1) / args.steps
+                cm[f"{c[0]}_p{c[1]}"] = {"ms": round(ms, 4),
+                                         "GB/s": round(call_bytes(c[0], n) / (ms * 1e-3) / 1e9, 1)}
+            compare[other] = cm
 
     # ---- end to end: host buffers through the C ABI ------------------------
     e2e = None

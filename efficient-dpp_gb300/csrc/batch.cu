@@ -60,8 +60,6 @@ union __align__(128) BatchSmem {
   struct {
     int32_t keys[kTile];
     int32_t vals[kTile];
-    int32_t okeys[kTile];  // the tile re-laid out in bucket order
-    int32_t ovals[kTile];
     uint16_t cnt16[kWarps * kMaxB];
     int32_t toff[kMaxB];
     int32_t gofs[kMaxB];
@@ -107,14 +105,13 @@ __device__ void block_exclusive_scan_inplace(int32_t *p, int64_t m, int32_t *wsu
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(kThreads, 3)
+__global__ void __launch_bounds__(kThreads)
     batch_kernel(const DevSeg *__restrict__ segs, const DevTask *__restrict__ tasks, int num_tasks,
                  const int32_t *__restrict__ in0, const int32_t *__restrict__ in1,
                  int32_t *__restrict__ out0, int32_t *__restrict__ out1, char *state,
                  Ctrl *ctrl, unsigned long long *ticket, unsigned *abort_flag, bool tma,
                  uint64_t timeout_ns, unsigned *fault) {
-  extern __shared__ __align__(128) unsigned char batch_smem[];
-  BatchSmem &sm = *reinterpret_cast<BatchSmem *>(batch_smem);
+  __shared__ BatchSmem sm;
   __shared__ alignas(8) uint64_t bar;
   __shared__ int s_task;
   __shared__ int s_flag;
@@ -126,6 +123,7 @@ __global__ void __launch_bounds__(kThreads, 3)
   __syncthreads();
   uint32_t phase = 0;
   const unsigned lt = lanemask_lt_b();
+
   // Thread 0 takes the next ticket early, once nothing can wait on the
   // current task any more: a SCAN tile after publishing its prefix, a SPLIT
   // tile once its histogram is ready, a GATHER tile at once (HIST tiles take
@@ -188,20 +186,22 @@ __global__ void __launch_bounds__(kThreads, 3)
       // ---- permutation gather tile, indices local to the segment ----
       take_next();
       const int32_t *src = in0 + seg.off;
-      constexpr int kPerT = kTile / kThreads;  // 16: every load in flight at once
-      int v[kPerT], idx[kPerT];
 #pragma unroll
-      for (int q = 0; q < kPerT; ++q) {
-        const int i = q * kThreads + t;
-        idx[q] = i < count ? in1[gbase + i] : -1;
-      }
+      for (int k = 0; k < kTile / kThreads; k += 4) {
+        int v[4], idx[4];
 #pragma unroll
-      for (int q = 0; q < kPerT; ++q)
-        v[q] = (idx[q] >= 0 && idx[q] < seg.len) ? __ldg(src + idx[q]) : 0;
+        for (int q = 0; q < 4; ++q) {
+          const int i = (k + q) * kThreads + t;
+          idx[q] = i < count ? in1[gbase + i] : -1;
+        }
 #pragma unroll
-      for (int q = 0; q < kPerT; ++q) {
-        const int i = q * kThreads + t;
-        if (idx[q] >= 0 && idx[q] < seg.len) out0[gbase + i] = v[q];
+        for (int q = 0; q < 4; ++q)
+          v[q] = (idx[q] >= 0 && idx[q] < seg.len) ? __ldg(src + idx[q]) : 0;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int i = (k + q) * kThreads + t;
+          if (idx[q] >= 0 && idx[q] < seg.len) out0[gbase + i] = v[q];
+        }
       }
     } else if (task.kind == kTaskHist) {
       // ---- bucket counts of a split tile ----
@@ -264,12 +264,14 @@ __global__ void __launch_bounds__(kThreads, 3)
         for (int i = t; i < kWarps * B; i += kThreads) sm.split.cnt16[i] = 0;
         __syncthreads();
         uint16_t *my = sm.split.cnt16 + w * B;
+        int32_t kk[kIters], vv[kIters];
         uint32_t rk[kIters / 2];
 #pragma unroll
         for (int it = 0; it < kIters; ++it) {
           const int pos = w * kSeg + it * 32 + lane;
           const bool valid = pos < count;
           const int32_t key = valid ? sm.split.keys[pos] : 0;
+          const int32_t val = valid ? sm.split.vals[pos] : 0;
           const int b = valid ? static_cast<int>(static_cast<unsigned>(key) & mask) : -1;
           const unsigned peers = __match_any_sync(0xffffffffu, b);
           const unsigned lower = peers & lt;
@@ -277,6 +279,8 @@ __global__ void __launch_bounds__(kThreads, 3)
           __syncwarp();
           if (valid && lower == 0u) my[b] = static_cast<uint16_t>(before + __popc(peers));
           __syncwarp();
+          kk[it] = key;
+          vv[it] = val;
           const uint32_t r = static_cast<uint32_t>(before + __popc(lower));
           if (it & 1) rk[it >> 1] |= r << 16;
           else rk[it >> 1] = r;
@@ -314,21 +318,20 @@ __global__ void __launch_bounds__(kThreads, 3)
         for (int it = 0; it < kIters; ++it) {
           const int pos = w * kSeg + it * 32 + lane;
           if (pos < count) {
-            const int32_t key = sm.split.keys[pos];
-            const int b = static_cast<int>(static_cast<unsigned>(key) & mask);
+            const int b = static_cast<int>(static_cast<unsigned>(kk[it]) & mask);
             const int r = static_cast<int>((rk[it >> 1] >> ((it & 1) * 16)) & 0xffffu);
             const int s = sm.split.toff[b] + sm.split.cnt16[w * B + b] + r;
-            sm.split.okeys[s] = key;
-            sm.split.ovals[s] = sm.split.vals[pos];
+            sm.split.keys[s] = kk[it];
+            sm.split.vals[s] = vv[it];
           }
         }
         __syncthreads();
         for (int s = t; s < count; s += kThreads) {
-          const int32_t key = sm.split.okeys[s];
+          const int32_t key = sm.split.keys[s];
           const int b = static_cast<int>(static_cast<unsigned>(key) & mask);
           const int64_t o = seg.off + sm.split.gofs[b] + s;
           out0[o] = key;
-          out1[o] = sm.split.ovals[s];
+          out1[o] = sm.split.vals[s];
         }
       }
     }
@@ -499,25 +502,22 @@ int edpp_batch_launch(const edpp_batch_plan *plan, const int32_t *in0, const int
   if (cudaMemsetAsync(w + p.off_ctrl, 0, p.off_state - p.off_ctrl + p.scan_state_bytes, st) !=
       cudaSuccess)
     return EDPP_ECUDA;
-  static std::once_flag attr_once[64];
-  static cudaError_t attr_err[64];
+  static std::once_flag occ_once[64];
+  static cudaError_t occ_err[64];
   static int resident[64];
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64) dev = 0;
-  std::call_once(attr_once[dev], [dev] {
-    attr_err[dev] = cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(sizeof(BatchSmem)));
-    if (attr_err[dev] == cudaSuccess)
-      attr_err[dev] = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident[dev], batch_kernel,
-                                                                    kThreads, sizeof(BatchSmem));
+  std::call_once(occ_once[dev], [dev] {
+    occ_err[dev] = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident[dev], batch_kernel,
+                                                                 kThreads, 0);
   });
-  if (attr_err[dev] != cudaSuccess) return EDPP_ECUDA;
+  if (occ_err[dev] != cudaSuccess) return EDPP_ECUDA;
   // blocks beyond what stays resident would only start once the queue is empty
   const int per_sm = std::max(1, std::min(p.blocks_per_sm, resident[dev]));
   int64_t blocks = static_cast<int64_t>(device_sm_count()) * per_sm;
   blocks = min64(blocks, static_cast<int64_t>(p.tasks.size()));
-  batch_kernel<<<static_cast<unsigned>(max64(blocks, 1)), kThreads, sizeof(BatchSmem), st>>>(
+  batch_kernel<<<static_cast<unsigned>(max64(blocks, 1)), kThreads, 0, st>>>(
       reinterpret_cast<const DevSeg *>(w + p.off_segs),
       reinterpret_cast<const DevTask *>(w + p.off_tasks), static_cast<int>(p.tasks.size()), in0,
       in1, out0, out1, w + p.off_state, reinterpret_cast<Ctrl *>(w + p.off_ctrl),
@@ -587,7 +587,7 @@ extern "C" int edpp_batch_autotune(const edpp_segment *segs, int num_segs, const
   }
   float best_t = 1e30f;
   int status = EDPP_OK;
-  for (int bps : {1, 2, 3}) {  // the launch clamps to the resident count (3)
+  for (int bps : {1, 2, 3, 4}) {  // the launch clamps to the resident count
     for (int defer : {0, 1, 2, 4}) {
       for (int lf : {0, 1}) {
         edpp_batch_tuning tu{bps, defer, lf, 0};

@@ -473,6 +473,433 @@ int part_run(const int32_t *in, int32_t *out, int64_t n, const int32_t *loc, int
   return launch_status();
 }
 
+// ==== shared-memory windows ("tiled" form) ===========================================
+//
+// The random side of the access moves from L2 into shared memory.  Pairs are
+// partitioned twice by their key's window -- coarse windows of 128 fine
+// windows, then fine windows of W = 2^14 (or 2^15) elements -- and one block
+// per fine window applies its pairs inside a shared-memory copy of that
+// window, so every global access is a streaming one:
+//
+//   scatter: count fine windows of loc -> scan -> partition {loc, in[i]} by
+//            coarse window -> refine by fine window -> apply: per window,
+//            out-window[loc - base] = value in shared memory, then store the
+//            written elements of the window (bitmap), coalesced
+//   gather:  count -> scan -> partition {loc, i} -> refine -> fetch: per
+//            window of in[], load it once and emit {i, in[loc]} grouped by
+//            the coarse window of i -> refine by fine window of i -> apply
+//
+// Streaming traffic per element: scatter ~48 B, gather ~80 B; no random
+// global access.  Within a window, pairs arrive in no particular order (the
+// per-window cursors are claimed atomically): every destination of a gather
+// is written once; a scatter with repeated destinations keeps one of the
+// colliding values, as the other forms do.
+constexpr int kWinThreads = 512;
+constexpr int kFineMinLog = 14;
+constexpr int kFineMaxLog = 15;      // 32 K int32 = 128 KB window
+constexpr int kMaxFine = 16384;      // count histogram: 64 KB of shared memory
+constexpr int kCoarseLogFan = 7;     // 128 fine windows per coarse window
+constexpr int kRefineSpan = kMaxWin; // fine windows one refine tile may span
+
+struct TPlan {
+  int fine_log = kFineMinLog, coarse_log = kFineMinLog + kCoarseLogFan, F = 1, C = 1;
+};
+
+TPlan tplan(int64_t n) {
+  TPlan p;
+  while (((n + (int64_t{1} << p.fine_log) - 1) >> p.fine_log) > kMaxFine) ++p.fine_log;
+  p.coarse_log = p.fine_log + kCoarseLogFan;
+  p.F = static_cast<int>(max64(1, (n + (int64_t{1} << p.fine_log) - 1) >> p.fine_log));
+  p.C = static_cast<int>(max64(1, (n + (int64_t{1} << p.coarse_log) - 1) >> p.coarse_log));
+  return p;
+}
+
+bool tiled_fits(int64_t n) { return tplan(n).fine_log <= kFineMaxLog; }
+
+__global__ void __launch_bounds__(kWinThreads)
+    win_count_kernel(const int32_t *__restrict__ loc, int64_t n, int fine_log, int F,
+                     uint32_t *__restrict__ cnt, bool vec) {
+  extern __shared__ uint32_t hist[];
+  for (int i = threadIdx.x; i < F; i += kWinThreads) hist[i] = 0;
+  __syncthreads();
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * kWinThreads;
+  const int64_t first = static_cast<int64_t>(blockIdx.x) * kWinThreads + threadIdx.x;
+  auto add = [&](int32_t l) {
+    if (static_cast<uint64_t>(static_cast<uint32_t>(l)) < static_cast<uint64_t>(n))
+      atomicAdd(&hist[static_cast<uint32_t>(l) >> fine_log], 1u);
+  };
+  int64_t done = 0;
+  if (vec) {
+    const int64_t n4 = n >> 2;
+    const int4 *l4 = reinterpret_cast<const int4 *>(loc);
+    for (int64_t i = first; i < n4; i += stride) {
+      const int4 q = __ldcs(l4 + i);
+      add(q.x);
+      add(q.y);
+      add(q.z);
+      add(q.w);
+    }
+    done = 4 * n4;
+  }
+  for (int64_t i = done + first; i < n; i += stride) add(loc[i]);
+  __syncthreads();
+  for (int i = threadIdx.x; i < F; i += kWinThreads)
+    if (hist[i]) atomicAdd(&cnt[i], hist[i]);
+}
+
+// start[f] = sum of cnt[0..f), start[F] = total; fill = start; cfill[c] =
+// start[c * 128]; gather also gets fill2[f] = f * W and cfill2[c] = c * 128 W.
+__global__ void __launch_bounds__(1024)
+    win_scan_kernel(const uint32_t *__restrict__ cnt, int F, int C, int fine_log, int coarse_log,
+                    uint32_t *__restrict__ start, uint32_t *__restrict__ fill,
+                    uint32_t *__restrict__ cfill, uint32_t *__restrict__ fill2,
+                    uint32_t *__restrict__ cfill2) {
+  __shared__ uint32_t wsum[32];
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  const int per = (F + 1023) / 1024;
+  const int lo = min(F, t * per), hi = min(F, lo + per);
+  uint32_t s = 0;
+  for (int i = lo; i < hi; ++i) s += cnt[i];
+  uint32_t incl = s;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d) incl += y;
+  }
+  if (lane == 31) wsum[w] = incl;
+  __syncthreads();
+  if (w == 0) {
+    const uint32_t x = wsum[lane];
+    uint32_t xi = x;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, xi, d);
+      if (lane >= d) xi += y;
+    }
+    wsum[lane] = xi - x;
+    if (lane == 31) start[F] = xi;
+  }
+  __syncthreads();
+  uint32_t run = wsum[w] + incl - s;
+  for (int i = lo; i < hi; ++i) {
+    start[i] = run;
+    fill[i] = run;
+    if ((i & ((1 << kCoarseLogFan) - 1)) == 0) cfill[i >> kCoarseLogFan] = run;
+    run += cnt[i];
+  }
+  if (fill2) {
+    for (int i = t; i < F; i += 1024) fill2[i] = static_cast<uint32_t>(i) << fine_log;
+    for (int c = t; c < C; c += 1024) cfill2[c] = static_cast<uint32_t>(c) << coarse_log;
+  }
+}
+
+// Append every pair of one tile to fine window (pair.x >> fine_log) at that
+// window's cursor.  The source is either the flat range [0, *total) or, with
+// region_log > 0, the regions [r << region_log, region_end[r]) (tiles of a
+// region beyond its end exit).  A tile whose fine windows span fewer than
+// kRefineSpan is grouped in shared memory and written as one run per window;
+// a wider tile (skewed keys) appends pair by pair.
+__global__ void __launch_bounds__(kThreads)
+    win_refine_kernel(const int2 *__restrict__ src, const uint32_t *__restrict__ total_p,
+                      const uint32_t *__restrict__ region_end, int region_log, int fine_log,
+                      uint32_t *__restrict__ fill, int2 *__restrict__ dst) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  int2 *stage = reinterpret_cast<int2 *>(smem);
+  uint32_t *scnt = reinterpret_cast<uint32_t *>(stage + kTile);
+  uint32_t *soff = scnt + kRefineSpan;
+  uint32_t *sgb = soff + kRefineSpan;
+  __shared__ uint32_t s_warp[16];
+  __shared__ int s_lo, s_hi;
+  int64_t lo_j, hi_j;
+  if (region_log > 0) {
+    const int tiles_per_region = 1 << (region_log - 12);  // kTile = 4096
+    const int64_t r = blockIdx.x / tiles_per_region;
+    lo_j = (r << region_log) + static_cast<int64_t>(blockIdx.x % tiles_per_region) * kTile;
+    hi_j = min64(lo_j + kTile, static_cast<int64_t>(region_end[r]));
+  } else {
+    lo_j = static_cast<int64_t>(blockIdx.x) * kTile;
+    hi_j = min64(lo_j + kTile, static_cast<int64_t>(*total_p));
+  }
+  if (lo_j >= hi_j) return;  // block-uniform
+  const int t = threadIdx.x;
+  if (t == 0) {
+    s_lo = INT_MAX;
+    s_hi = -1;
+  }
+  for (int i = t; i < kRefineSpan; i += kThreads) scnt[i] = 0;
+  int2 pr[kPer];
+  int fid[kPer];
+  int my_lo = INT_MAX, my_hi = -1;
+#pragma unroll
+  for (int k = 0; k < kPer / 2; ++k) {
+    const int64_t j = lo_j + static_cast<int64_t>(k * kThreads + t) * 2;
+    int4 q = make_int4(-1, 0, -1, 0);
+    if (j + 1 < hi_j) q = __ldcs(reinterpret_cast<const int4 *>(src + j));
+    else if (j < hi_j) { const int2 a = src[j]; q.x = a.x; q.y = a.y; }
+    pr[2 * k] = make_int2(q.x, q.y);
+    pr[2 * k + 1] = make_int2(q.z, q.w);
+    fid[2 * k] = j < hi_j ? (q.x >> fine_log) : -1;
+    fid[2 * k + 1] = j + 1 < hi_j ? (q.z >> fine_log) : -1;
+  }
+#pragma unroll
+  for (int e = 0; e < kPer; ++e)
+    if (fid[e] >= 0) {
+      my_lo = min(my_lo, fid[e]);
+      my_hi = max(my_hi, fid[e]);
+    }
+#pragma unroll
+  for (int m = 16; m >= 1; m >>= 1) {
+    my_lo = min(my_lo, __shfl_xor_sync(0xffffffffu, my_lo, m));
+    my_hi = max(my_hi, __shfl_xor_sync(0xffffffffu, my_hi, m));
+  }
+  __syncthreads();
+  if ((t & 31) == 0) {
+    atomicMin(&s_lo, my_lo);
+    atomicMax(&s_hi, my_hi);
+  }
+  __syncthreads();
+  const int lo = s_lo, span = s_hi - s_lo + 1;
+  if (span > kRefineSpan) {  // skewed tile: one cursor claim per pair
+#pragma unroll
+    for (int e = 0; e < kPer; ++e)
+      if (fid[e] >= 0) dst[atomicAdd(&fill[fid[e]], 1u)] = pr[e];
+    return;
+  }
+  const unsigned lt = lanemask_lt();
+  int rank[kPer], w[kPer];
+#pragma unroll
+  for (int e = 0; e < kPer; ++e) {
+    w[e] = fid[e] >= 0 ? fid[e] - lo : -1;
+    rank[e] = rank_in_window(w[e], scnt, lt);
+  }
+  __syncthreads();
+  const uint32_t total = block_scan_counts(scnt, soff, span, s_warp);
+  for (int i = t; i < span; i += kThreads)
+    if (scnt[i]) sgb[i] = atomicAdd(&fill[lo + i], scnt[i]);
+#pragma unroll
+  for (int e = 0; e < kPer; ++e)
+    if (w[e] >= 0) stage[soff[w[e]] + rank[e]] = pr[e];
+  __syncthreads();
+  for (uint32_t s = t; s < total; s += kThreads) {
+    const int2 p = stage[s];
+    const int ww = (p.x >> fine_log) - lo;
+    dst[sgb[ww] + (s - soff[ww])] = p;
+  }
+}
+
+// One block per fine window f: pairs [start[f], start[f+1]) (or, without
+// start, [f << fine_log, fill_end[f])) are {index, value} with index inside
+// the window; they are applied in shared memory and the written elements of
+// the window are stored (a bitmap marks them; untouched elements keep their
+// old value in `out`).
+__global__ void __launch_bounds__(kWinThreads)
+    win_apply_kernel(const int2 *__restrict__ pairs, const uint32_t *__restrict__ start,
+                     const uint32_t *__restrict__ fill_end, int fine_log, int64_t n,
+                     int32_t *__restrict__ out, bool vec_out) {
+  extern __shared__ __align__(16) int32_t win[];
+  const int W = 1 << fine_log;
+  uint32_t *bits = reinterpret_cast<uint32_t *>(win + W);
+  const int f = blockIdx.x;
+  const int64_t base = static_cast<int64_t>(f) << fine_log;
+  const int len = static_cast<int>(min64(W, n - base));
+  const int64_t lo = start ? start[f] : base;
+  const int64_t hi = start ? start[f + 1] : fill_end[f];
+  const int t = threadIdx.x;
+  for (int i = t; i < (W >> 5); i += kWinThreads) bits[i] = 0u;
+  __syncthreads();
+  auto put = [&](int2 p) {
+    const int rel = static_cast<int>(p.x - base);
+    win[rel] = p.y;
+    atomicOr(&bits[rel >> 5], 1u << (rel & 31));
+  };
+  // pairs: scalar head to an even index, then two per 16-byte load
+  int64_t j = lo;
+  if ((j & 1) && j < hi) {
+    if (t == 0) put(pairs[j]);
+    ++j;
+  }
+  const int64_t nv = (hi - j) >> 1;
+  const int4 *p4 = reinterpret_cast<const int4 *>(pairs + j);
+  for (int64_t v = t; v < nv; v += 4 * kWinThreads) {
+    int4 q[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (v + u * kWinThreads < nv) q[u] = __ldcs(p4 + v + u * kWinThreads);
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (v + u * kWinThreads < nv) {
+        put(make_int2(q[u].x, q[u].y));
+        put(make_int2(q[u].z, q[u].w));
+      }
+  }
+  if (t == 0 && j + 2 * nv < hi) put(pairs[j + 2 * nv]);
+  __syncthreads();
+  for (int e0 = 4 * t; e0 < len; e0 += 4 * kWinThreads) {
+    const uint32_t nib = (bits[e0 >> 5] >> (e0 & 31)) & 0xFu;
+    if (nib == 0xFu && vec_out && e0 + 3 < len) {
+      __stcs(reinterpret_cast<int4 *>(out + base + e0), *reinterpret_cast<const int4 *>(win + e0));
+    } else {
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (e0 + k < len && ((nib >> k) & 1u)) out[base + e0 + k] = win[e0 + k];
+    }
+  }
+}
+
+// Gather fetch: one block per fine window f of in[]; the window is loaded
+// once into shared memory, and each pair {loc, i} of the window becomes
+// {i, in[loc]}, appended to the coarse window of i (cursors cfill2).
+__global__ void __launch_bounds__(kThreads)
+    win_fetch_kernel(const int2 *__restrict__ pairs, const uint32_t *__restrict__ start,
+                     const int32_t *__restrict__ in, int64_t n, int fine_log, int coarse_log,
+                     int C, uint32_t *__restrict__ cfill2, int2 *__restrict__ dst, bool vec_in) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int W = 1 << fine_log;
+  int32_t *win = reinterpret_cast<int32_t *>(smem);
+  int2 *stage = reinterpret_cast<int2 *>(win + W);
+  uint32_t *scnt = reinterpret_cast<uint32_t *>(stage + kTile);
+  uint32_t *soff = scnt + C;
+  uint32_t *sgb = soff + C;
+  __shared__ uint32_t s_warp[16];
+  const int f = blockIdx.x, t = threadIdx.x;
+  const int64_t base = static_cast<int64_t>(f) << fine_log;
+  const int len = static_cast<int>(min64(W, n - base));
+  const int64_t lo = start[f], hi = start[f + 1];
+  if (lo >= hi) return;  // block-uniform
+  if (vec_in) {
+    const int4 *s4 = reinterpret_cast<const int4 *>(in + base);
+    for (int q = t; q < (len >> 2); q += kThreads) reinterpret_cast<int4 *>(win)[q] = __ldcs(s4 + q);
+    for (int e = (len & ~3) + t; e < len; e += kThreads) win[e] = in[base + e];
+  } else {
+    for (int e = t; e < len; e += kThreads) win[e] = in[base + e];
+  }
+  const unsigned lt = lanemask_lt();
+  for (int64_t c0 = lo; c0 < hi; c0 += kTile) {
+    for (int i = t; i < C; i += kThreads) scnt[i] = 0;
+    __syncthreads();  // also: window loaded, previous tile's stage consumed
+    int2 pr[kPer];
+    int w[kPer], rank[kPer];
+#pragma unroll
+    for (int e = 0; e < kPer; ++e) {
+      const int64_t j = c0 + static_cast<int64_t>(e) * kThreads + t;
+      const bool valid = j < hi;
+      const int2 a = valid ? pairs[j] : make_int2(0, 0);
+      pr[e] = make_int2(a.y, valid ? win[a.x - base] : 0);  // {i, value}
+      w[e] = valid ? (a.y >> coarse_log) : -1;
+      rank[e] = rank_in_window(w[e], scnt, lt);
+    }
+    __syncthreads();
+    flush_runs<kPer>(pr, w, rank, C, coarse_log, scnt, soff, sgb, s_warp, stage, cfill2, dst);
+    __syncthreads();
+  }
+}
+
+size_t refine_smem() { return static_cast<size_t>(kTile) * 8 + 3 * 4 * static_cast<size_t>(kRefineSpan); }
+size_t apply_smem(int fine_log) { return (size_t{4} << fine_log) + (size_t{1} << fine_log) / 8; }
+size_t fetch_smem(int fine_log, int C) {
+  return (size_t{4} << fine_log) + static_cast<size_t>(kTile) * 8 + 3 * 4 * static_cast<size_t>(C);
+}
+
+int ensure_win_attrs() {
+  static std::once_flag once[64];
+  static int st[64];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  std::call_once(once[dev], [dev] {
+    auto set = [](const void *k, size_t b) {
+      return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(b));
+    };
+    cudaError_t e = set(reinterpret_cast<const void *>(win_count_kernel), 4 * kMaxFine);
+    if (e == cudaSuccess) e = set(reinterpret_cast<const void *>(win_refine_kernel), refine_smem());
+    if (e == cudaSuccess) e = set(reinterpret_cast<const void *>(win_apply_kernel), apply_smem(kFineMaxLog));
+    if (e == cudaSuccess)
+      e = set(reinterpret_cast<const void *>(win_fetch_kernel), fetch_smem(kFineMaxLog, 1 << (31 - kFineMaxLog - kCoarseLogFan)));
+    if (e == cudaSuccess)
+      e = set(reinterpret_cast<const void *>(part_partition_kernel<true>), part_smem(kMaxWin));
+    if (e == cudaSuccess)
+      e = set(reinterpret_cast<const void *>(part_partition_kernel<false>), part_smem(kMaxWin));
+    st[dev] = e == cudaSuccess ? EDPP_OK : EDPP_ECUDA;
+  });
+  return st[dev];
+}
+
+struct TLayout {
+  size_t cnt, start, fill, cfill, fill2, cfill2, pairs_a, pairs_b, bytes;
+};
+
+TLayout tlayout_of(int64_t n, const TPlan &p, bool gather) {
+  TLayout L{};
+  size_t o = kHdr;
+  auto take = [&](size_t b) {
+    const size_t at = o;
+    o += round_up(b, 256);
+    return at;
+  };
+  L.cnt = take(4 * static_cast<size_t>(p.F));
+  L.start = take(4 * static_cast<size_t>(p.F + 1));
+  L.fill = take(4 * static_cast<size_t>(p.F));
+  L.cfill = take(4 * static_cast<size_t>(p.C));
+  L.fill2 = gather ? take(4 * static_cast<size_t>(p.F)) : 0;
+  L.cfill2 = gather ? take(4 * static_cast<size_t>(p.C)) : 0;
+  L.pairs_a = take(8 * static_cast<size_t>(n));
+  L.pairs_b = take(8 * static_cast<size_t>(n));
+  L.bytes = o;
+  return L;
+}
+
+template <bool kScatter>
+int tiled_run(const int32_t *in, int32_t *out, int64_t n, const int32_t *loc, int pass, void *ws,
+              size_t ws_bytes, void *stream) {
+  if (n < 0 || pass < 0) return EDPP_EINVAL;
+  if (n == 0) return EDPP_OK;
+  if (!in || !out || !loc) return EDPP_EINVAL;
+  if (n > INT32_MAX) return EDPP_EINVAL;
+  if (!tiled_fits(n)) return part_run<kScatter>(in, out, n, loc, 0, ws, ws_bytes, stream);
+  const TPlan p = tplan(n);
+  const TLayout L = tlayout_of(n, p, !kScatter);
+  if (!ws || ws_bytes < L.bytes) return EDPP_ENOMEM;
+  int s = ensure_win_attrs();
+  if (s != EDPP_OK) return s;
+  cudaStream_t st = as_stream(stream);
+  char *w = static_cast<char *>(ws);
+  auto *cnt = reinterpret_cast<uint32_t *>(w + L.cnt);
+  auto *start = reinterpret_cast<uint32_t *>(w + L.start);
+  auto *fill = reinterpret_cast<uint32_t *>(w + L.fill);
+  auto *cfill = reinterpret_cast<uint32_t *>(w + L.cfill);
+  auto *fill2 = kScatter ? nullptr : reinterpret_cast<uint32_t *>(w + L.fill2);
+  auto *cfill2 = kScatter ? nullptr : reinterpret_cast<uint32_t *>(w + L.cfill2);
+  auto *pa = reinterpret_cast<int2 *>(w + L.pairs_a);
+  auto *pb = reinterpret_cast<int2 *>(w + L.pairs_b);
+  if (cudaMemsetAsync(cnt, 0, 4 * static_cast<size_t>(p.F), st) != cudaSuccess) return EDPP_ECUDA;
+  const int sms = device_sm_count();
+  const bool vec_loc = aligned16(loc);
+  const bool vec_in = aligned16(in);
+  const int64_t cblocks = min64(static_cast<int64_t>(sms) * 2, (n + 4 * kWinThreads - 1) / (4 * kWinThreads));
+  win_count_kernel<<<static_cast<unsigned>(max64(cblocks, 1)), kWinThreads, 4 * p.F, st>>>(
+      loc, n, p.fine_log, p.F, cnt, vec_loc);
+  win_scan_kernel<<<1, 1024, 0, st>>>(cnt, p.F, p.C, p.fine_log, p.coarse_log, start, fill, cfill,
+                                      fill2, cfill2);
+  const int64_t tiles = (n + kTile - 1) / kTile;
+  part_partition_kernel<kScatter><<<static_cast<unsigned>(tiles), kThreads, part_smem(p.C), st>>>(
+      loc, in, n, p.coarse_log, p.C, cfill, pa, vec_loc && (!kScatter || vec_in));
+  win_refine_kernel<<<static_cast<unsigned>(tiles), kThreads, refine_smem(), st>>>(
+      pa, start + p.F, nullptr, 0, p.fine_log, fill, pb);
+  if (kScatter) {
+    win_apply_kernel<<<static_cast<unsigned>(p.F), kWinThreads, apply_smem(p.fine_log), st>>>(
+        pb, start, nullptr, p.fine_log, n, out, aligned16(out));
+  } else {
+    win_fetch_kernel<<<static_cast<unsigned>(p.F), kThreads, fetch_smem(p.fine_log, p.C), st>>>(
+        pb, start, in, n, p.fine_log, p.coarse_log, p.C, cfill2, pa, vec_in);
+    const int64_t rtiles = static_cast<int64_t>(p.C) << (p.coarse_log - 12);
+    win_refine_kernel<<<static_cast<unsigned>(rtiles), kThreads, refine_smem(), st>>>(
+        pa, nullptr, cfill2, p.coarse_log, p.fine_log, fill2, pb);
+    win_apply_kernel<<<static_cast<unsigned>(p.F), kWinThreads, apply_smem(p.fine_log), st>>>(
+        pb, nullptr, fill2, p.fine_log, n, out, aligned16(out));
+  }
+  return launch_status();
+}
+
 }  // namespace
 }  // namespace edpp
 
@@ -496,6 +923,28 @@ int edpp_gather_i32_ws(const int32_t *in, int32_t *out, int64_t length, const in
 int edpp_scatter_i32_ws(const int32_t *in, int32_t *out, int64_t length, const int32_t *loc,
                         int pass, void *ws, size_t ws_bytes, void *stream) {
   return edpp::part_run<true>(in, out, length, loc, pass, ws, ws_bytes, stream);
+}
+
+size_t edpp_gather_tiled_workspace_size(int64_t length) {
+  if (length <= 0) return 0;
+  if (!edpp::tiled_fits(length)) return edpp_gather_workspace_size(length, 0);
+  return edpp::tlayout_of(length, edpp::tplan(length), true).bytes;
+}
+
+size_t edpp_scatter_tiled_workspace_size(int64_t length) {
+  if (length <= 0) return 0;
+  if (!edpp::tiled_fits(length)) return edpp_scatter_workspace_size(length, 0);
+  return edpp::tlayout_of(length, edpp::tplan(length), false).bytes;
+}
+
+int edpp_gather_i32_tiled(const int32_t *in, int32_t *out, int64_t length, const int32_t *loc,
+                          int pass, void *ws, size_t ws_bytes, void *stream) {
+  return edpp::tiled_run<false>(in, out, length, loc, pass, ws, ws_bytes, stream);
+}
+
+int edpp_scatter_i32_tiled(const int32_t *in, int32_t *out, int64_t length, const int32_t *loc,
+                           int pass, void *ws, size_t ws_bytes, void *stream) {
+  return edpp::tiled_run<true>(in, out, length, loc, pass, ws, ws_bytes, stream);
 }
 
 }  // extern "C"

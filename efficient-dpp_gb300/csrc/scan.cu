@@ -96,91 +96,6 @@ __global__ void __launch_bounds__(kThreads)
   S::store(out, base, count, c, vec_out);
 }
 
-// Persistent form: a block keeps taking tiles from the ticket and issues the
-// bulk copy of its next tile before scanning the current one, so loads
-// overlap the look-back.  Holding one ticket ahead never blocks progress:
-// the smallest unfinished tile is always some block's current tile and it
-// only waits on smaller, finished tiles.
-constexpr int kLookbackBlocksPerSm = 6;
-
-template <typename T, bool kInclusive>
-__global__ void __launch_bounds__(kThreads)
-    scan_lookback_persistent_kernel(const T *in, T *out, int64_t n, int64_t num_tiles,
-                                    unsigned long long *ticket, LookbackState<T> st,
-                                    int64_t ticket_base, bool tma, bool vec_out,
-                                    uint64_t timeout_ns, unsigned *fault) {
-  using S = TS<T>;
-  constexpr int kTile = S::kTile;
-  __shared__ alignas(128) T buf[2][kTile];
-  __shared__ typename S::Shared sh;
-  __shared__ alignas(8) uint64_t bar[2];
-  __shared__ int64_t s_next;
-  unsigned *abort_flag = reinterpret_cast<unsigned *>(ticket + 1);
-  auto count_of = [&](int64_t t) { return static_cast<int>(min64(kTile, n - t * kTile)); };
-
-  if (threadIdx.x == 0) {
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
-    fence_mbar_init();
-    s_next = static_cast<int64_t>(atomicAdd(ticket, 1ull)) + ticket_base;
-  }
-  __syncthreads();
-  int64_t cur = s_next;
-  int slot = 0;
-  uint32_t phase = 0;  // bit s: parity of the next completion of bar[s]
-  uint32_t bulk_cur = 0;
-  if (cur < num_tiles)
-    bulk_cur = stage_tile<T, kTile, kThreads>(buf[0], in + cur * kTile, count_of(cur), tma, &bar[0]);
-  while (cur < num_tiles) {
-    // The next ticket is taken only once this tile's inclusive prefix is
-    // published: a block never holds an unstarted tile while it waits in a
-    // look-back, so no tile waits behind another block's wait (holding it
-    // earlier chains the waits and serialises the whole scan).  Its bulk
-    // copy then overlaps this tile's output phase.
-    const int count = count_of(cur);
-    bool failed = false;
-    if (bulk_cur) {
-      failed = !mbar_wait_bounded(&bar[slot], (phase >> slot) & 1u, timeout_ns, fault);
-      phase ^= 1u << slot;
-    }
-    if (__syncthreads_or(failed)) {  // also: sh and s_next of the last tile are consumed
-      atomicOr(abort_flag, 1u);
-      break;
-    }
-    Chunk<T> c[kChunks];
-    T wex[kChunks];
-    S::phase1(buf[slot], c, wex, sh);
-    __syncthreads();
-    if (threadIdx.x < 32) {
-      const int lane = threadIdx.x;
-      const T agg = S::phase2_warp0(sh, lane);
-      T prefix = zero_of<T>();
-      bool ok = true;
-      if (cur == 0) {
-        if (lane == 0) st.publish(0, kFlagIncl, agg);
-      } else {
-        prefix = lookback_warp<T>(st, cur, agg, lane, timeout_ns, fault, abort_flag, ok);
-      }
-      if (lane == 0) {
-        sh.prefix = ok ? prefix : zero_of<T>();
-        s_next = static_cast<int64_t>(atomicAdd(ticket, 1ull)) + ticket_base;
-      }
-    }
-    __syncthreads();
-    if (fault_raised(abort_flag)) break;  // a failed call writes nothing further
-    const int64_t nxt = s_next;
-    uint32_t bulk_nxt = 0;
-    if (nxt < num_tiles)  // buf[slot ^ 1] was consumed by the previous tile's phase 1
-      bulk_nxt = stage_tile<T, kTile, kThreads>(buf[slot ^ 1], in + nxt * kTile, count_of(nxt), tma,
-                                                &bar[slot ^ 1]);
-    S::template phase3<kInclusive>(c, wex, sh, sh.prefix);
-    S::store(out, cur * kTile, count, c, vec_out);
-    cur = nxt;
-    bulk_cur = bulk_nxt;
-    slot ^= 1;
-  }
-}
-
 // ---- RTS / SSA building blocks ----------------------------------------------
 
 // Per-block sum of the block's contiguous range [b*per, min((b+1)*per, n)).
@@ -401,9 +316,10 @@ int scan_impl(const T *in, T *out, int64_t n, int algo, void *ws, size_t ws_byte
     if (cudaMemsetAsync(ws, 0, need, st) != cudaSuccess) return EDPP_ECUDA;
     LookbackState<T> state;
     state.bind(w + kHeader, tiles);
-    const int64_t blocks =
-        max64(1, min64(tiles, static_cast<int64_t>(device_sm_count()) * kLookbackBlocksPerSm));
-    scan_lookback_persistent_kernel<T, kInclusive><<<static_cast<unsigned>(blocks), kThreads, 0, st>>>(
+    // One block per tile, tiles taken in ticket order.  (A persistent form
+    // that prefetches its next tile measured 10-15% slower: look-backs of
+    // blocks that advance in lockstep see fewer published prefixes.)
+    scan_lookback_kernel<T, kInclusive><<<static_cast<unsigned>(tiles), kThreads, 0, st>>>(
         in, out, n, tiles, reinterpret_cast<unsigned long long *>(w), state, ticket_base, tma,
         vec_out, timeout_ns, fault);
     return launch_status();

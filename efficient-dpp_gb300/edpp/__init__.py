@@ -67,6 +67,10 @@ SIGNATURES = {
     "edpp_access_wg_i32": (_I, [_VP, _I64, _VP, _I, _I, _VP, _VP, _VP]),
     "edpp_cache_heat_i32": (_I, [_VP, _I64, _I, _I, _VP]),
     "edpp_local_scan_i32": (_I, [_VP, _VP, _I, _I, _I, _VP]),
+    "edpp_gather_tiled_workspace_size": (_SZ, [_I64]),
+    "edpp_scatter_tiled_workspace_size": (_SZ, [_I64]),
+    "edpp_gather_i32_tiled": (_I, [_VP, _VP, _I64, _VP, _I, _VP, _SZ, _VP]),
+    "edpp_scatter_i32_tiled": (_I, [_VP, _VP, _I64, _VP, _I, _VP, _SZ, _VP]),
     "edpp_stream_copy_f32": (_I, [_VP, _VP, _I64, _VP]),
     "edpp_stream_scale_f32": (_I, [_VP, _VP, _F, _I64, _VP]),
     "edpp_stream_add_f32": (_I, [_VP, _VP, _VP, _I64, _VP]),
@@ -191,18 +195,27 @@ def _gs(kind, inp, loc, passes, out, method, ws):
     if method == "sweep":
         f = lib().edpp_gather_i32 if kind == "gather" else lib().edpp_scatter_i32
         check(f(_p(inp), _p(out), n, _p(loc), int(passes), st), kind)
-    elif method == "partition":
-        need = gs_workspace_bytes(kind, n, passes)
+    elif method in ("partition", "tiled"):
+        need = gs_workspace_bytes(kind, n, passes, method)
         if ws is None:
             ws = workspace(need, loc.device)
-        f = lib().edpp_gather_i32_ws if kind == "gather" else lib().edpp_scatter_i32_ws
+        if method == "partition":
+            f = lib().edpp_gather_i32_ws if kind == "gather" else lib().edpp_scatter_i32_ws
+        else:
+            f = lib().edpp_gather_i32_tiled if kind == "gather" else lib().edpp_scatter_i32_tiled
         check(f(_p(inp), _p(out), n, _p(loc), int(passes), _p(ws), ws.numel(), st), kind)
     else:
         raise ValueError(method)
     return out
 
 
-def gs_workspace_bytes(kind: str, n: int, passes: int) -> int:
+def gs_workspace_bytes(kind: str, n: int, passes: int, method: str = "partition") -> int:
+    if method == "tiled":
+        f = (lib().edpp_gather_tiled_workspace_size if kind == "gather"
+             else lib().edpp_scatter_tiled_workspace_size)
+        return f(int(n))
+    if method == "sweep":
+        return 0
     f = lib().edpp_gather_workspace_size if kind == "gather" else lib().edpp_scatter_workspace_size
     return f(int(n), int(passes))
 
@@ -210,7 +223,8 @@ def gs_workspace_bytes(kind: str, n: int, passes: int) -> int:
 def gather(inp, loc, passes: int = 1, out=None, method: str = "sweep", ws=None):
     """out[i] = inp[loc[i]].  method "sweep": one launch per pass window, each
     reading all of loc (the reference's schedule); "partition": the windows
-    as partitions (passes=0 sizes them to L2)."""
+    as partitions (passes=0 sizes them to L2); "tiled": shared-memory
+    windows (the result does not depend on passes)."""
     return _gs("gather", inp, loc, passes, out, method, ws)
 
 

@@ -134,6 +134,22 @@ int edpp_scatter_i32_ws(const int32_t *in, int32_t *out, int64_t length,
                         const int32_t *loc, int pass, void *ws, size_t ws_bytes,
                         void *stream);
 
+/* Shared-memory-window gather / scatter: the same results again, for every
+ * pass count (pass >= 0 is accepted for the same signature; the windows are
+ * fixed by shared memory, 2^14 or 2^15 elements).  Requests are partitioned
+ * twice by window (128 coarse windows, then fine windows) and one block per
+ * fine window serves them inside a shared-memory copy of that window, so no
+ * global access is random.  length <= 2^29; longer arrays take the
+ * L2-window path (pass 0) with the workspace sized for it. */
+size_t edpp_gather_tiled_workspace_size(int64_t length);
+size_t edpp_scatter_tiled_workspace_size(int64_t length);
+int edpp_gather_i32_tiled(const int32_t *in, int32_t *out, int64_t length,
+                          const int32_t *loc, int pass, void *ws, size_t ws_bytes,
+                          void *stream);
+int edpp_scatter_i32_tiled(const int32_t *in, int32_t *out, int64_t length,
+                           const int32_t *loc, int pass, void *ws, size_t ws_bytes,
+                           void *stream);
+
 /* ---- global scan -------------------------------------------------------- */
 
 /* Bytes of workspace a scan of `length` elements of `dtype` with `algo`

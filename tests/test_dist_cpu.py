@@ -55,3 +55,4 @@ def test_step_accounting():
     assert step == n * (10 * 12 + 8 + 8 + 12 + 12)
     assert sum(bench.call_launches(c, p, "sweep") for c, p in calls) == 2 * 31 + 4
     assert sum(bench.call_launches(c, p, "partition") for c, p in calls) == 2 + 4 * 5 + 4 * 4 + 4
+    assert sum(bench.call_launches(c, p, "tiled") for c, p in calls) == 5 * 7 + 5 * 5 + 4

@@ -10,7 +10,7 @@ pytestmark = pytest.mark.gpu
 PASSES = [1, 2, 4, 8, 16]
 
 
-METHODS = ["sweep", "partition"]
+METHODS = ["sweep", "partition", "tiled"]
 
 
 @pytest.mark.parametrize("method", METHODS)
@@ -85,8 +85,8 @@ def test_config2a_full_size_properties(cuda, edpp, method):
     loc = to_dev(edpp.gen_permutation(n, 2))
     inp = cuda.arange(n, dtype=cuda.int32, device="cuda")
     ws = None
-    if method == "partition":
-        ws = edpp.workspace(max(edpp.gs_workspace_bytes("gather", n, p) for p in PASSES))
+    if method != "sweep":
+        ws = edpp.workspace(max(edpp.gs_workspace_bytes("gather", n, p, method) for p in PASSES))
     for passes in PASSES:
         g = edpp.gather(inp, loc, passes, method=method, ws=ws)
         assert cuda.equal(g, loc), passes
@@ -95,6 +95,38 @@ def test_config2a_full_size_properties(cuda, edpp, method):
         back = edpp.gather(s, loc, passes, method=method, ws=ws)
         assert cuda.equal(back, inp), passes
         del s, back
+
+
+@pytest.mark.parametrize("n", [16384, 16385, (1 << 21) + 7, 3 * (1 << 20) + 1])
+def test_tiled_skewed_indices(cuda, edpp, orc, n):
+    # every index in a few windows (one window's pairs exceed a refine tile's
+    # span, the per-pair cursor path), plus invalid ones
+    rng = np.random.default_rng(n)
+    loc = rng.integers(0, min(n, 3000), n).astype(np.int32)
+    loc[::7] = rng.integers(0, n, len(loc[::7])).astype(np.int32)
+    loc[3::11] = -5
+    inp = edpp.gen_uniform_i32(n, 4, -2**31, 2**31 - 1)
+    out0 = np.full(n, 99, np.int32)
+    g = to_host(edpp.gather(to_dev(inp), to_dev(loc), 1, out=to_dev(out0), method="tiled"))
+    np.testing.assert_array_equal(g, orc.gather(inp, loc, 1, out=out0))
+    # scatter through a permutation, destinations drawn from two windows first
+    perm = edpp.gen_permutation(n, 9)
+    order = np.argsort(perm % 5, kind="stable")
+    perm = perm[order]
+    s = to_host(edpp.scatter(to_dev(inp), to_dev(perm), 4, out=to_dev(out0), method="tiled"))
+    np.testing.assert_array_equal(s, orc.scatter(inp, perm, 4, out=out0))
+
+
+def test_tiled_wide_windows(cuda, edpp):
+    # above 2^28 elements the windows grow to 2^15 (128 KB of shared memory)
+    n = (1 << 28) + 5
+    loc = to_dev(edpp.gen_permutation(n, 2))
+    inp = cuda.arange(n, dtype=cuda.int32, device="cuda")
+    ws = edpp.workspace(edpp.gs_workspace_bytes("gather", n, 1, "tiled"))
+    g = edpp.gather(inp, loc, 1, method="tiled", ws=ws)
+    assert cuda.equal(g, loc)
+    s = edpp.scatter(inp, loc, 1, method="tiled", ws=ws)
+    assert cuda.equal(edpp.gather(s, loc, 1, method="tiled", ws=ws), inp)
 
 
 def test_against_reference_cuda_kernels(cuda, edpp, orc):
