@@ -211,9 +211,7 @@ __global__ void __launch_bounds__(kThreads)
       for (int i0 = 0; i0 < kTile; i0 += kThreads) {
         const int i = i0 + t;
         const bool valid = i < count;
-        const int b = valid ? static_cast<int>(static_cast<unsigned>(in0[gbase + i]) & mask) : -1;
-        const unsigned peers = __match_any_sync(0xffffffffu, b);
-        if (valid && (peers & lt) == 0u) atomicAdd(&sm.hist.cnt[b], static_cast<uint32_t>(__popc(peers)));
+        if (valid) atomicAdd(&sm.hist.cnt[static_cast<unsigned>(in0[gbase + i]) & mask], 1u);
       }
       __syncthreads();
       int32_t *his = reinterpret_cast<int32_t *>(state + seg.state);
@@ -264,6 +262,7 @@ __global__ void __launch_bounds__(kThreads)
         for (int i = t; i < kWarps * B; i += kThreads) sm.split.cnt16[i] = 0;
         __syncthreads();
         uint16_t *my = sm.split.cnt16 + w * B;
+        const int kbits = 31 - __clz(B);
         int32_t kk[kIters], vv[kIters];
         uint32_t rk[kIters / 2];
 #pragma unroll
@@ -273,7 +272,8 @@ __global__ void __launch_bounds__(kThreads)
           const int32_t key = valid ? sm.split.keys[pos] : 0;
           const int32_t val = valid ? sm.split.vals[pos] : 0;
           const int b = valid ? static_cast<int>(static_cast<unsigned>(key) & mask) : -1;
-          const unsigned peers = __match_any_sync(0xffffffffu, b);
+          const unsigned peers =
+              match_low_bits(static_cast<unsigned>(b), kbits, __ballot_sync(0xffffffffu, valid));
           const unsigned lower = peers & lt;
           const uint16_t before = valid ? my[b] : 0;
           __syncwarp();

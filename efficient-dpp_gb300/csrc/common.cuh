@@ -11,6 +11,20 @@
 
 namespace edpp {
 
+// Lanes of the calling warp whose value has the same low `bits` bits as this
+// lane's, restricted to `among`; one vote per bit (all 32 lanes must call).
+// Used instead of __match_any_sync, which on this GPU issues far slower.
+__device__ __forceinline__ unsigned match_low_bits(unsigned v, int bits, unsigned among) {
+  unsigned peers = among;
+  for (int i = 0; i < bits; ++i) {
+    const unsigned one = (v >> i) & 1u;
+    const unsigned bb = __ballot_sync(0xffffffffu, one);
+    peers &= one ? bb : ~bb;
+  }
+  return peers;
+}
+
+
 // Number of SMs on a GB300 (two dies of 76).  Grids are sized as multiples of
 // the SM count the runtime reports; this is only the fallback.
 constexpr int kGb300Sms = 152;

@@ -52,15 +52,13 @@ __device__ __forceinline__ int ld_nc(const int32_t *p) {
   return v;
 }
 
-// Rank of this lane's element among the tile's elements of window w
-// (-1: invalid), by warp-aggregated shared-memory atomics.
-__device__ __forceinline__ int rank_in_window(int w, uint32_t *scnt, unsigned lt) {
-  const unsigned peers = __match_any_sync(0xffffffffu, w);
-  const int leader = __ffs(peers) - 1;
-  uint32_t base = 0;
-  if (w >= 0 && (peers & lt) == 0u) base = atomicAdd(&scnt[w], static_cast<uint32_t>(__popc(peers)));
-  base = __shfl_sync(0xffffffffu, base, leader);
-  return w >= 0 ? static_cast<int>(base) + __popc(peers & lt) : -1;
+// A slot for this lane's element among the tile's elements of window w (-1:
+// invalid): one shared-memory atomic per element.  Slots within a window come
+// in no particular order, which no caller depends on.  (Grouping lanes with
+// __match_any_sync first costs several times more: on this GPU the match
+// instruction, not memory, bounded these kernels.)
+__device__ __forceinline__ int rank_in_window(int w, uint32_t *scnt, unsigned) {
+  return w >= 0 ? static_cast<int>(atomicAdd(&scnt[w], 1u)) : -1;
 }
 
 // Block-wide exclusive scan of scnt[0..nwin) into soff[], returns total.
@@ -118,8 +116,6 @@ __global__ void __launch_bounds__(kThreads)
   if (vec) {
     const int64_t n4 = n >> 2;
     const int4 *l4 = reinterpret_cast<const int4 *>(loc);
-    // Trip count is uniform across the warp (rounded up), lanes past the end
-    // contribute invalid elements, so __match_any_sync sees the full warp.
     const int64_t base0 = static_cast<int64_t>(blockIdx.x) * kThreads;
     for (int64_t b = base0; b < n4; b += stride) {
       const int64_t i = b + threadIdx.x;

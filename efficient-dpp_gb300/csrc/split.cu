@@ -6,8 +6,7 @@
 // cuda/test_split.cu:149-186), re-planned for GB300:
 //
 //  1. hist:    one block per tile of kTile elements counts its buckets with
-//              warp-aggregated shared-memory atomics (__match_any_sync groups
-//              the lanes of a bucket; one leader adds the group size) and
+//              shared-memory atomics (one per element) and
 //              writes column t of the bucket-major matrix his[b*T + t], the
 //              layout of WI/WG_histogram (split_kernel.cl:370,451) and of
 //              warp_histogram (cuda/test_split.cu:48).
@@ -17,7 +16,7 @@
 //              index of bucket b's elements from tile t.
 //  3. scatter: one block per tile stages the tile in shared memory by TMA
 //              bulk copy; every warp ranks its contiguous 1/WARPS of the tile
-//              in input order (peer group from __match_any_sync, rank = popc
+//              in input order (peer group from one vote per bucket bit, rank = popc
 //              of lower peers + the warp's running count of the bucket, kept
 //              as 16-bit counters in shared memory); ranks of all warps are
 //              combined per bucket, the tile is re-laid out in shared memory
@@ -64,12 +63,9 @@ __global__ void __launch_bounds__(kHistThreads)
   const int64_t t = blockIdx.x;
   const int64_t base = t * kTile;
   const int count = static_cast<int>(min64(kTile, n - base));
-  const unsigned lt = lanemask_lt();
 
   auto add = [&](bool valid, int32_t key) {
-    const int b = valid ? static_cast<int>((static_cast<unsigned>(key) >> shift) & mask) : -1;
-    const unsigned peers = __match_any_sync(0xffffffffu, b);
-    if (valid && (peers & lt) == 0u) atomicAdd(&cnt[b], static_cast<uint32_t>(__popc(peers)));
+    if (valid) atomicAdd(&cnt[(static_cast<unsigned>(key) >> shift) & mask], 1u);
   };
 
   if (LAYOUT != EDPP_KVS_AOS && vec && count == kTile) {
@@ -182,6 +178,7 @@ __global__ void __launch_bounds__(THREADS)
 
   // -- rank: warp w owns tile positions [w*kSeg, (w+1)*kSeg), in order --
   const unsigned lt = lanemask_lt();
+  const int kbits = 31 - __clz(buckets);
   uint16_t *my_cnt = cnt16 + w * buckets;
   int32_t kk[C::kIters];
   int32_t vv[C::kIters];
@@ -202,7 +199,7 @@ __global__ void __launch_bounds__(THREADS)
       }
     }
     const int b = valid ? static_cast<int>((static_cast<unsigned>(key) >> shift) & mask) : -1;
-    const unsigned peers = __match_any_sync(0xffffffffu, b);
+    const unsigned peers = match_low_bits(static_cast<unsigned>(b), kbits, __ballot_sync(0xffffffffu, valid));
     const unsigned lower = peers & lt;
     const uint16_t before = valid ? my_cnt[b] : 0;
     __syncwarp();
