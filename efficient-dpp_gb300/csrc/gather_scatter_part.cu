@@ -595,7 +595,7 @@ __global__ void __launch_bounds__(1024)
 // region beyond its end exit).  A tile whose fine windows span fewer than
 // kRefineSpan is grouped in shared memory and written as one run per window;
 // a wider tile (skewed keys) appends pair by pair.
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 3)
     win_refine_kernel(const int2 *__restrict__ src, const uint32_t *__restrict__ total_p,
                       const uint32_t *__restrict__ region_end, int region_log, int fine_log,
                       uint32_t *__restrict__ fill, int2 *__restrict__ dst) {
@@ -662,11 +662,11 @@ __global__ void __launch_bounds__(kThreads)
     return;
   }
   const unsigned lt = lanemask_lt();
-  int rank[kPer], w[kPer];
+  int rank[kPer];
 #pragma unroll
   for (int e = 0; e < kPer; ++e) {
-    w[e] = fid[e] >= 0 ? fid[e] - lo : -1;
-    rank[e] = rank_in_window(w[e], scnt, lt);
+    fid[e] = fid[e] >= 0 ? fid[e] - lo : -1;  // window relative to the tile's first
+    rank[e] = rank_in_window(fid[e], scnt, lt);
   }
   __syncthreads();
   const uint32_t total = block_scan_counts(scnt, soff, span, s_warp);
@@ -674,7 +674,7 @@ __global__ void __launch_bounds__(kThreads)
     if (scnt[i]) sgb[i] = atomicAdd(&fill[lo + i], scnt[i]);
 #pragma unroll
   for (int e = 0; e < kPer; ++e)
-    if (w[e] >= 0) stage[soff[w[e]] + rank[e]] = pr[e];
+    if (fid[e] >= 0) stage[soff[fid[e]] + rank[e]] = pr[e];
   __syncthreads();
   for (uint32_t s = t; s < total; s += kThreads) {
     const int2 p = stage[s];
