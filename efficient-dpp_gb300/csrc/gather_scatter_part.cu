@@ -495,7 +495,6 @@ constexpr int kFineMinLog = 14;
 constexpr int kFineMaxLog = 15;      // 32 K int32 = 128 KB window
 constexpr int kMaxFine = 16384;      // count histogram: 64 KB of shared memory
 constexpr int kCoarseLogFan = 7;     // 128 fine windows per coarse window
-constexpr int kRefineSpan = kMaxWin; // fine windows one refine tile may span
 
 struct TPlan {
   int fine_log = kFineMinLog, coarse_log = kFineMinLog + kCoarseLogFan, F = 1, C = 1;
@@ -590,96 +589,174 @@ __global__ void __launch_bounds__(1024)
 }
 
 // Append every pair of one tile to fine window (pair.x >> fine_log) at that
-// window's cursor.  The source is either the flat range [0, *total) or, with
-// region_log > 0, the regions [r << region_log, region_end[r]) (tiles of a
-// region beyond its end exit).  A tile whose fine windows span fewer than
-// kRefineSpan is grouped in shared memory and written as one run per window;
-// a wider tile (skewed keys) appends pair by pair.
-__global__ void __launch_bounds__(kThreads, 3)
+// window's cursor.  The tiles ("slots") are either the flat range [0, *total)
+// cut into kTile pairs, or, with region_log > 0, each region
+// [r << region_log, region_end[r]) cut the same way (slots past a region's
+// end are empty).  Persistent blocks take slots blockIdx, +gridDim, ...; the
+// slot after next is copied into shared memory by TMA while the current one
+// is processed, so loads stay in flight through the block's grouping work.
+// A slot whose fine windows span at most kRefineSpan is grouped in shared
+// memory (the landed input buffer is reused as the staging area) and written
+// as one run per window; a wider one (skewed keys) appends pair by pair.
+constexpr int kRefineSpan = 512;
+constexpr int kRefineBlocksPerSm = 3;
+
+__device__ __forceinline__ void refine_range(int64_t slot, const uint32_t *total_p,
+                                             const uint32_t *region_end, int region_log,
+                                             int64_t &lo, int64_t &hi) {
+  if (region_log > 0) {
+    const int shift = region_log - 12;  // kTile = 4096 = 2^12
+    const int64_t r = slot >> shift;
+    lo = (r << region_log) + ((slot & ((int64_t{1} << shift) - 1)) << 12);
+    hi = min64(lo + kTile, static_cast<int64_t>(region_end[r]));
+  } else {
+    lo = slot * kTile;
+    hi = min64(lo + kTile, static_cast<int64_t>(*total_p));
+  }
+}
+
+// Thread 0: start the bulk copy of the even part of [lo, hi) into buf.
+__device__ __forceinline__ void refine_issue(const int2 *src, int64_t lo, int64_t hi, int2 *buf,
+                                             uint64_t *bar) {
+  const uint32_t even = static_cast<uint32_t>(hi - lo) & ~1u;
+  if (lo < hi && even) {
+    mbar_arrive_expect_tx(bar, even * 8u);
+    tma_load_1d(buf, src + lo, even * 8u, bar);
+  }
+}
+
+__global__ void __launch_bounds__(kThreads, kRefineBlocksPerSm)
     win_refine_kernel(const int2 *__restrict__ src, const uint32_t *__restrict__ total_p,
                       const uint32_t *__restrict__ region_end, int region_log, int fine_log,
-                      uint32_t *__restrict__ fill, int2 *__restrict__ dst) {
+                      int64_t slots, uint32_t *__restrict__ fill, int2 *__restrict__ dst,
+                      uint64_t timeout_ns, unsigned *fault) {
   extern __shared__ __align__(16) unsigned char smem[];
-  int2 *stage = reinterpret_cast<int2 *>(smem);
-  uint32_t *scnt = reinterpret_cast<uint32_t *>(stage + kTile);
+  int2 *bufs = reinterpret_cast<int2 *>(smem);  // [2][kTile]
+  uint32_t *scnt = reinterpret_cast<uint32_t *>(bufs + 2 * kTile);
   uint32_t *soff = scnt + kRefineSpan;
   uint32_t *sgb = soff + kRefineSpan;
+  __shared__ alignas(8) uint64_t bar[2];
   __shared__ uint32_t s_warp[16];
   __shared__ int s_lo, s_hi;
-  int64_t lo_j, hi_j;
-  if (region_log > 0) {
-    const int tiles_per_region = 1 << (region_log - 12);  // kTile = 4096
-    const int64_t r = blockIdx.x / tiles_per_region;
-    lo_j = (r << region_log) + static_cast<int64_t>(blockIdx.x % tiles_per_region) * kTile;
-    hi_j = min64(lo_j + kTile, static_cast<int64_t>(region_end[r]));
-  } else {
-    lo_j = static_cast<int64_t>(blockIdx.x) * kTile;
-    hi_j = min64(lo_j + kTile, static_cast<int64_t>(*total_p));
-  }
-  if (lo_j >= hi_j) return;  // block-uniform
   const int t = threadIdx.x;
+  const int64_t G = gridDim.x;
   if (t == 0) {
-    s_lo = INT_MAX;
-    s_hi = -1;
-  }
-  for (int i = t; i < kRefineSpan; i += kThreads) scnt[i] = 0;
-  int2 pr[kPer];
-  int fid[kPer];
-  int my_lo = INT_MAX, my_hi = -1;
-#pragma unroll
-  for (int k = 0; k < kPer / 2; ++k) {
-    const int64_t j = lo_j + static_cast<int64_t>(k * kThreads + t) * 2;
-    int4 q = make_int4(-1, 0, -1, 0);
-    if (j + 1 < hi_j) q = __ldcs(reinterpret_cast<const int4 *>(src + j));
-    else if (j < hi_j) { const int2 a = src[j]; q.x = a.x; q.y = a.y; }
-    pr[2 * k] = make_int2(q.x, q.y);
-    pr[2 * k + 1] = make_int2(q.z, q.w);
-    fid[2 * k] = j < hi_j ? (q.x >> fine_log) : -1;
-    fid[2 * k + 1] = j + 1 < hi_j ? (q.z >> fine_log) : -1;
-  }
-#pragma unroll
-  for (int e = 0; e < kPer; ++e)
-    if (fid[e] >= 0) {
-      my_lo = min(my_lo, fid[e]);
-      my_hi = max(my_hi, fid[e]);
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+    for (int k = 0; k < 2; ++k) {
+      const int64_t sk = blockIdx.x + k * G;
+      if (sk < slots) {
+        int64_t lo, hi;
+        refine_range(sk, total_p, region_end, region_log, lo, hi);
+        refine_issue(src, lo, hi, bufs + k * kTile, &bar[k]);
+      }
     }
-#pragma unroll
-  for (int m = 16; m >= 1; m >>= 1) {
-    my_lo = min(my_lo, __shfl_xor_sync(0xffffffffu, my_lo, m));
-    my_hi = max(my_hi, __shfl_xor_sync(0xffffffffu, my_hi, m));
   }
   __syncthreads();
-  if ((t & 31) == 0) {
-    atomicMin(&s_lo, my_lo);
-    atomicMax(&s_hi, my_hi);
-  }
-  __syncthreads();
-  const int lo = s_lo, span = s_hi - s_lo + 1;
-  if (span > kRefineSpan) {  // skewed tile: one cursor claim per pair
-#pragma unroll
-    for (int e = 0; e < kPer; ++e)
-      if (fid[e] >= 0) dst[atomicAdd(&fill[fid[e]], 1u)] = pr[e];
-    return;
-  }
   const unsigned lt = lanemask_lt();
-  int rank[kPer];
+  uint32_t phase = 0;  // bit b: parity of bar[b]'s next completion
+  int b = 0;
+  int64_t slot = blockIdx.x;
+  bool failed = false;
+  for (; slot < slots; slot += G, b ^= 1) {
+    int64_t lo, hi;
+    refine_range(slot, total_p, region_end, region_log, lo, hi);
+    int2 *buf = bufs + b * kTile;
+    if (lo < hi) {  // block-uniform
+      const uint32_t cnt = static_cast<uint32_t>(hi - lo);
+      bool bad = false;
+      if (cnt & ~1u) {
+        bad = !mbar_wait_bounded(&bar[b], (phase >> b) & 1u, timeout_ns, fault);
+        phase ^= 1u << b;
+      }
+      if (t == 0) {
+        if (cnt & 1u) buf[cnt - 1] = src[hi - 1];
+        s_lo = INT_MAX;
+        s_hi = -1;
+      }
+      for (int i = t; i < kRefineSpan; i += kThreads) scnt[i] = 0;
+      if (__syncthreads_or(bad)) {
+        failed = true;
+        break;
+      }
+      int2 pr[kPer];
+      int fid[kPer];
+      int my_lo = INT_MAX, my_hi = -1;
 #pragma unroll
-  for (int e = 0; e < kPer; ++e) {
-    fid[e] = fid[e] >= 0 ? fid[e] - lo : -1;  // window relative to the tile's first
-    rank[e] = rank_in_window(fid[e], scnt, lt);
+      for (int k = 0; k < kPer / 2; ++k) {
+        const uint32_t j = static_cast<uint32_t>(k * kThreads + t) * 2u;
+        int4 q = make_int4(0, 0, 0, 0);
+        if (j + 1 < cnt) q = *reinterpret_cast<const int4 *>(buf + j);
+        else if (j < cnt) { const int2 a = buf[j]; q.x = a.x; q.y = a.y; }
+        pr[2 * k] = make_int2(q.x, q.y);
+        pr[2 * k + 1] = make_int2(q.z, q.w);
+        fid[2 * k] = j < cnt ? (q.x >> fine_log) : -1;
+        fid[2 * k + 1] = j + 1 < cnt ? (q.z >> fine_log) : -1;
+      }
+#pragma unroll
+      for (int e = 0; e < kPer; ++e)
+        if (fid[e] >= 0) {
+          my_lo = min(my_lo, fid[e]);
+          my_hi = max(my_hi, fid[e]);
+        }
+#pragma unroll
+      for (int m = 16; m >= 1; m >>= 1) {
+        my_lo = min(my_lo, __shfl_xor_sync(0xffffffffu, my_lo, m));
+        my_hi = max(my_hi, __shfl_xor_sync(0xffffffffu, my_hi, m));
+      }
+      if ((t & 31) == 0) {
+        atomicMin(&s_lo, my_lo);
+        atomicMax(&s_hi, my_hi);
+      }
+      __syncthreads();  // also: every read of buf is done
+      const int wlo = s_lo, span = s_hi - s_lo + 1;
+      if (span > kRefineSpan) {  // skewed slot: one cursor claim per pair
+#pragma unroll
+        for (int e = 0; e < kPer; ++e)
+          if (fid[e] >= 0) dst[atomicAdd(&fill[fid[e]], 1u)] = pr[e];
+      } else {
+        int rank[kPer];
+#pragma unroll
+        for (int e = 0; e < kPer; ++e) {
+          fid[e] = fid[e] >= 0 ? fid[e] - wlo : -1;
+          rank[e] = rank_in_window(fid[e], scnt, lt);
+        }
+        __syncthreads();
+        const uint32_t total = block_scan_counts(scnt, soff, span, s_warp);
+        for (int i = t; i < span; i += kThreads)
+          if (scnt[i]) sgb[i] = atomicAdd(&fill[wlo + i], scnt[i]);
+#pragma unroll
+        for (int e = 0; e < kPer; ++e)
+          if (fid[e] >= 0) buf[soff[fid[e]] + rank[e]] = pr[e];
+        __syncthreads();
+        for (uint32_t q = t; q < total; q += kThreads) {
+          const int2 p = buf[q];
+          const int ww = (p.x >> fine_log) - wlo;
+          dst[sgb[ww] + (q - soff[ww])] = p;
+        }
+      }
+      fence_proxy_async_smem();  // generic accesses of buf before the next bulk copy into it
+      __syncthreads();
+    }
+    if (t == 0) {
+      const int64_t sn = slot + 2 * G;
+      if (sn < slots) {
+        int64_t lo2, hi2;
+        refine_range(sn, total_p, region_end, region_log, lo2, hi2);
+        refine_issue(src, lo2, hi2, buf, &bar[b]);
+      }
+    }
   }
-  __syncthreads();
-  const uint32_t total = block_scan_counts(scnt, soff, span, s_warp);
-  for (int i = t; i < span; i += kThreads)
-    if (scnt[i]) sgb[i] = atomicAdd(&fill[lo + i], scnt[i]);
-#pragma unroll
-  for (int e = 0; e < kPer; ++e)
-    if (fid[e] >= 0) stage[soff[fid[e]] + rank[e]] = pr[e];
-  __syncthreads();
-  for (uint32_t s = t; s < total; s += kThreads) {
-    const int2 p = stage[s];
-    const int ww = (p.x >> fine_log) - lo;
-    dst[sgb[ww] + (s - soff[ww])] = p;
+  if (failed) {
+    // let the other buffer's copy (slot + G), if one was started, land
+    const int64_t sn = slot + G;
+    if (sn < slots) {
+      int64_t lo2, hi2;
+      refine_range(sn, total_p, region_end, region_log, lo2, hi2);
+      if (lo2 < hi2 && ((static_cast<uint32_t>(hi2 - lo2) & ~1u) != 0u))
+        mbar_wait_bounded(&bar[b ^ 1], (phase >> (b ^ 1)) & 1u, timeout_ns, fault);
+    }
   }
 }
 
@@ -790,7 +867,9 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
-size_t refine_smem() { return static_cast<size_t>(kTile) * 8 + 3 * 4 * static_cast<size_t>(kRefineSpan); }
+size_t refine_smem() {
+  return 2 * static_cast<size_t>(kTile) * 8 + 3 * 4 * static_cast<size_t>(kRefineSpan);
+}
 size_t apply_smem(int fine_log) { return (size_t{4} << fine_log) + (size_t{1} << fine_log) / 8; }
 size_t fetch_smem(int fine_log, int C) {
   return (size_t{4} << fine_log) + static_cast<size_t>(kTile) * 8 + 3 * 4 * static_cast<size_t>(C);
@@ -879,8 +958,11 @@ int tiled_run(const int32_t *in, int32_t *out, int64_t n, const int32_t *loc, in
   const int64_t tiles = (n + kTile - 1) / kTile;
   part_partition_kernel<kScatter><<<static_cast<unsigned>(tiles), kThreads, part_smem(p.C), st>>>(
       loc, in, n, p.coarse_log, p.C, cfill, pa, vec_loc && (!kScatter || vec_in));
-  win_refine_kernel<<<static_cast<unsigned>(tiles), kThreads, refine_smem(), st>>>(
-      pa, start + p.F, nullptr, 0, p.fine_log, fill, pb);
+  unsigned *fault = fault_word();
+  if (!fault) return EDPP_ECUDA;
+  const int64_t rblocks = static_cast<int64_t>(sms) * kRefineBlocksPerSm;
+  win_refine_kernel<<<static_cast<unsigned>(min64(tiles, rblocks)), kThreads, refine_smem(), st>>>(
+      pa, start + p.F, nullptr, 0, p.fine_log, tiles, fill, pb, kDefaultWaitNs, fault);
   if (kScatter) {
     win_apply_kernel<<<static_cast<unsigned>(p.F), kWinThreads, apply_smem(p.fine_log), st>>>(
         pb, start, nullptr, p.fine_log, n, out, aligned16(out));
@@ -888,8 +970,8 @@ int tiled_run(const int32_t *in, int32_t *out, int64_t n, const int32_t *loc, in
     win_fetch_kernel<<<static_cast<unsigned>(p.F), kThreads, fetch_smem(p.fine_log, p.C), st>>>(
         pb, start, in, n, p.fine_log, p.coarse_log, p.C, cfill2, pa, vec_in);
     const int64_t rtiles = static_cast<int64_t>(p.C) << (p.coarse_log - 12);
-    win_refine_kernel<<<static_cast<unsigned>(rtiles), kThreads, refine_smem(), st>>>(
-        pa, nullptr, cfill2, p.coarse_log, p.fine_log, fill2, pb);
+    win_refine_kernel<<<static_cast<unsigned>(min64(rtiles, rblocks)), kThreads, refine_smem(), st>>>(
+        pa, nullptr, cfill2, p.coarse_log, p.fine_log, rtiles, fill2, pb, kDefaultWaitNs, fault);
     win_apply_kernel<<<static_cast<unsigned>(p.F), kWinThreads, apply_smem(p.fine_log), st>>>(
         pb, nullptr, fill2, p.fine_log, n, out, aligned16(out));
   }
