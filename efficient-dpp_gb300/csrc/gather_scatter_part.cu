@@ -232,6 +232,103 @@ __global__ void __launch_bounds__(kThreads)
   flush_runs<kPer>(pr, w, rank, nwin, log_w, scnt, soff, sgb, s_warp, stage, fill, pairs);
 }
 
+// Pipelined form of the partition for 16-byte-aligned loc (and in): persistent
+// blocks take tiles blockIdx, +gridDim, ...; the tile after next is copied
+// into shared memory by TMA (loc, and in for a scatter, on one barrier) while
+// the current one is grouped; the landed buffer then serves as the staging
+// area of the runs.  Same output as part_partition_kernel.
+template <bool kScatter>
+__global__ void __launch_bounds__(kThreads, 2)
+    part_partition_pipe_kernel(const int32_t *__restrict__ loc, const int32_t *__restrict__ in,
+                               int64_t n, int log_w, int nwin, uint32_t *__restrict__ fill,
+                               int2 *__restrict__ pairs, uint64_t timeout_ns, unsigned *fault) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  int32_t *bufs = reinterpret_cast<int32_t *>(smem);  // [2][2 * kTile]: loc | in
+  uint32_t *scnt = reinterpret_cast<uint32_t *>(bufs + 4 * kTile);
+  uint32_t *soff = scnt + nwin;
+  uint32_t *sgb = soff + nwin;
+  __shared__ alignas(8) uint64_t bar[2];
+  __shared__ uint32_t s_warp[16];
+  const int t = threadIdx.x;
+  const int64_t G = gridDim.x;
+  const int64_t tiles = (n + kTile - 1) / kTile;
+  // bytes of tile `tl` that go by bulk copy (per array); the rest by plain loads
+  auto bulk_of = [&](int64_t tl) {
+    return static_cast<uint32_t>(min64(kTile, n - tl * kTile) * 4) & ~15u;
+  };
+  auto issue = [&](int64_t tl, int32_t *buf, uint64_t *b) {  // thread 0
+    const uint32_t bytes = bulk_of(tl);
+    if (!bytes) return;
+    mbar_arrive_expect_tx(b, kScatter ? 2 * bytes : bytes);
+    tma_load_1d(buf, loc + tl * kTile, bytes, b);
+    if (kScatter) tma_load_1d(buf + kTile, in + tl * kTile, bytes, b);
+  };
+  if (t == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+    for (int k = 0; k < 2; ++k)
+      if (blockIdx.x + k * G < tiles) issue(blockIdx.x + k * G, bufs + k * 2 * kTile, &bar[k]);
+  }
+  __syncthreads();
+  const unsigned lt = lanemask_lt();
+  uint32_t phase = 0;
+  int b = 0;
+  int64_t tl = blockIdx.x;
+  bool failed = false;
+  for (; tl < tiles; tl += G, b ^= 1) {
+    int32_t *buf = bufs + b * 2 * kTile;
+    const int64_t base = tl * kTile;
+    const int count = static_cast<int>(min64(kTile, n - base));
+    const uint32_t bytes = bulk_of(tl);
+    bool bad = false;
+    if (bytes) {
+      bad = !mbar_wait_bounded(&bar[b], (phase >> b) & 1u, timeout_ns, fault);
+      phase ^= 1u << b;
+    }
+    for (int i = static_cast<int>(bytes / 4) + t; i < count; i += kThreads) {
+      buf[i] = loc[base + i];
+      if (kScatter) buf[kTile + i] = in[base + i];
+    }
+    for (int i = t; i < nwin; i += kThreads) scnt[i] = 0;
+    if (__syncthreads_or(bad)) {
+      failed = true;
+      break;
+    }
+    int2 pr[kPer];
+    int w[kPer], rank[kPer];
+#pragma unroll
+    for (int k = 0; k < kPer / 4; ++k) {
+      const int i0 = (k * kThreads + t) * 4;
+      const int4 l = *reinterpret_cast<const int4 *>(buf + i0);
+      int4 v = make_int4(0, 0, 0, 0);
+      if (kScatter) v = *reinterpret_cast<const int4 *>(buf + kTile + i0);
+      const int32_t ls[4] = {l.x, l.y, l.z, l.w};
+      const int32_t vs[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int e = 4 * k + q;
+        const bool valid = (i0 + q < count) && ls[q] >= 0 && static_cast<int64_t>(ls[q]) < n;
+        w[e] = valid ? (ls[q] >> log_w) : -1;
+        pr[e] = make_int2(ls[q], kScatter ? vs[q] : static_cast<int32_t>(base + i0 + q));
+        rank[e] = rank_in_window(w[e], scnt, lt);
+      }
+    }
+    __syncthreads();  // counts complete; every read of buf done
+    flush_runs<kPer>(pr, w, rank, nwin, log_w, scnt, soff, sgb, s_warp,
+                     reinterpret_cast<int2 *>(buf), fill, pairs);
+    fence_proxy_async_smem();  // generic accesses of buf before the next bulk copy into it
+    __syncthreads();
+    if (t == 0 && tl + 2 * G < tiles) issue(tl + 2 * G, buf, &bar[b]);
+  }
+  if (failed && tl + G < tiles && bulk_of(tl + G))  // let the other buffer's copy land
+    mbar_wait_bounded(&bar[b ^ 1], (phase >> (b ^ 1)) & 1u, timeout_ns, fault);
+}
+
+size_t part_pipe_smem(int nwin) {
+  return 4 * static_cast<size_t>(kTile) * 4 + 3 * 4 * static_cast<size_t>(nwin);
+}
+
 // ---- gather fetch: ordered sweep, v = in[loc], regroup by destination --------------
 __global__ void __launch_bounds__(kThreads)
     part_fetch_kernel(const int2 *__restrict__ pairs, const uint32_t *__restrict__ total_p,
@@ -410,10 +507,41 @@ int ensure_attrs() {
     if (d < 0 || d >= 64) d = 0;
     int s = set_smem(part_partition_kernel<false>);
     if (s == EDPP_OK) s = set_smem(part_partition_kernel<true>);
+    if (s == EDPP_OK)
+      s = cuda_status(cudaFuncSetAttribute(part_partition_pipe_kernel<false>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           static_cast<int>(part_pipe_smem(kMaxWin))));
+    if (s == EDPP_OK)
+      s = cuda_status(cudaFuncSetAttribute(part_partition_pipe_kernel<true>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           static_cast<int>(part_pipe_smem(kMaxWin))));
     if (s == EDPP_OK) s = set_smem(part_fetch_kernel);
     st[d] = s;
   });
   return st[dev];
+}
+
+// The partition stage: pipelined when loc (and in) are 16-byte aligned.
+template <bool kScatter>
+int launch_partition(const int32_t *loc, const int32_t *in, int64_t n, int log_w, int nwin,
+                     uint32_t *fill, int2 *pairs, bool vec, cudaStream_t st) {
+  const int64_t tiles = (n + kTile - 1) / kTile;
+  if (!vec) {
+    part_partition_kernel<kScatter><<<static_cast<unsigned>(tiles), kThreads, part_smem(nwin), st>>>(
+        loc, in, n, log_w, nwin, fill, pairs, false);
+    return launch_status();
+  }
+  unsigned *fault = fault_word();
+  if (!fault) return EDPP_ECUDA;
+  const size_t smem = part_pipe_smem(nwin);
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, part_partition_pipe_kernel<kScatter>,
+                                                    kThreads, smem) != cudaSuccess)
+    return EDPP_ECUDA;
+  const int64_t blocks = min64(tiles, static_cast<int64_t>(device_sm_count()) * max64(per_sm, 1));
+  part_partition_pipe_kernel<kScatter><<<static_cast<unsigned>(blocks), kThreads, smem, st>>>(
+      loc, in, n, log_w, nwin, fill, pairs, kDefaultWaitNs, fault);
+  return launch_status();
 }
 
 template <bool kScatter>
@@ -450,10 +578,9 @@ int part_run(const int32_t *in, int32_t *out, int64_t n, const int32_t *loc, int
   part_count_kernel<<<static_cast<unsigned>(max64(count_blocks, 1)), kThreads, 4 * p.nwin, st>>>(
       loc, n, p.log_w, p.nwin, cnt, vec_loc);
   part_bases_kernel<<<1, kThreads, 0, st>>>(cnt, fill, fill2, p.nwin, p.w_elems, total);
-  const int64_t tiles = (n + kTile - 1) / kTile;
   const size_t smem = part_smem(p.nwin);
-  part_partition_kernel<kScatter><<<static_cast<unsigned>(tiles), kThreads, smem, st>>>(
-      loc, in, n, p.log_w, p.nwin, fill, pairs, vec);
+  s = launch_partition<kScatter>(loc, in, n, p.log_w, p.nwin, fill, pairs, vec, st);
+  if (s != EDPP_OK) return s;
   const unsigned persist = static_cast<unsigned>(sms) * 4;
   if (kScatter) {
     const int64_t chunks = (n + kChunk - 1) / kChunk;  // upper bound; total <= n
@@ -935,6 +1062,7 @@ int tiled_run(const int32_t *in, int32_t *out, int64_t n, const int32_t *loc, in
   const TLayout L = tlayout_of(n, p, !kScatter);
   if (!ws || ws_bytes < L.bytes) return EDPP_ENOMEM;
   int s = ensure_win_attrs();
+  if (s == EDPP_OK) s = ensure_attrs();
   if (s != EDPP_OK) return s;
   cudaStream_t st = as_stream(stream);
   char *w = static_cast<char *>(ws);
@@ -956,8 +1084,9 @@ int tiled_run(const int32_t *in, int32_t *out, int64_t n, const int32_t *loc, in
   win_scan_kernel<<<1, 1024, 0, st>>>(cnt, p.F, p.C, p.fine_log, p.coarse_log, start, fill, cfill,
                                       fill2, cfill2);
   const int64_t tiles = (n + kTile - 1) / kTile;
-  part_partition_kernel<kScatter><<<static_cast<unsigned>(tiles), kThreads, part_smem(p.C), st>>>(
-      loc, in, n, p.coarse_log, p.C, cfill, pa, vec_loc && (!kScatter || vec_in));
+  s = launch_partition<kScatter>(loc, in, n, p.coarse_log, p.C, cfill, pa,
+                                 vec_loc && (!kScatter || vec_in), st);
+  if (s != EDPP_OK) return s;
   unsigned *fault = fault_word();
   if (!fault) return EDPP_ECUDA;
   const int64_t rblocks = static_cast<int64_t>(sms) * kRefineBlocksPerSm;

@@ -88,35 +88,28 @@ template <typename T> struct LookbackState<T, true> {
   }
 };
 
-// 64-bit values: value slots for the aggregate and the inclusive prefix, and
-// a flag published with release semantics after its value.
+// 64-bit values: two 64-bit words per tile, {flag, low half} and {flag, high
+// half}, each written and read single-copy atomically (one round trip for a
+// read, like the 32-bit form).  A reader that sees different flags in the
+// two words caught a tile between its aggregate and its inclusive prefix and
+// reports "not yet published", so it reads again.
 template <typename T> struct LookbackState<T, false> {
-  uint32_t *flags;
-  uint64_t *agg;
-  uint64_t *incl;
-  static size_t bytes(int64_t tiles) {
-    return round_up(static_cast<size_t>(tiles) * 4, 256) +
-           2 * round_up(static_cast<size_t>(tiles) * 8, 256);
-  }
-  __host__ __device__ void bind(void *p, int64_t tiles) {
-    char *c = static_cast<char *>(p);
-    flags = reinterpret_cast<uint32_t *>(c);
-    c += round_up(static_cast<size_t>(tiles) * 4, 256);
-    agg = reinterpret_cast<uint64_t *>(c);
-    c += round_up(static_cast<size_t>(tiles) * 8, 256);
-    incl = reinterpret_cast<uint64_t *>(c);
-  }
+  uint64_t *words;
+  static size_t bytes(int64_t tiles) { return round_up(static_cast<size_t>(tiles) * 16, 256); }
+  __host__ __device__ void bind(void *p, int64_t /*tiles*/) { words = static_cast<uint64_t *>(p); }
   __device__ __forceinline__ void publish(int64_t tile, uint32_t flag, T v) const {
     uint64_t bits;
     memcpy(&bits, &v, 8);
-    st_relaxed_u64((flag == kFlagAgg ? agg : incl) + tile, bits);
-    st_release_u32(flags + tile, flag);
+    const uint64_t f = static_cast<uint64_t>(flag) << 32;
+    st_relaxed_u64(words + 2 * tile, f | (bits & 0xffffffffull));
+    st_relaxed_u64(words + 2 * tile + 1, f | (bits >> 32));
   }
   __device__ __forceinline__ void read(int64_t tile, uint32_t &flag, T &v) const {
-    flag = ld_acquire_u32(flags + tile);
-    uint64_t bits = 0;
-    if (flag == kFlagAgg) bits = ld_relaxed_u64(agg + tile);
-    else if (flag == kFlagIncl) bits = ld_relaxed_u64(incl + tile);
+    const uint64_t lo = ld_relaxed_u64(words + 2 * tile);
+    const uint64_t hi = ld_relaxed_u64(words + 2 * tile + 1);
+    const uint32_t f0 = static_cast<uint32_t>(lo >> 32), f1 = static_cast<uint32_t>(hi >> 32);
+    flag = f0 == f1 ? f0 : kFlagNone;
+    const uint64_t bits = (hi << 32) | (lo & 0xffffffffull);
     memcpy(&v, &bits, 8);
   }
 };
