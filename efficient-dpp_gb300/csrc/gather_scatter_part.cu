@@ -952,7 +952,8 @@ __global__ void __launch_bounds__(kWinThreads)
 __global__ void __launch_bounds__(kThreads)
     win_fetch_kernel(const int2 *__restrict__ pairs, const uint32_t *__restrict__ start,
                      const int32_t *__restrict__ in, int64_t n, int fine_log, int coarse_log,
-                     int C, uint32_t *__restrict__ cfill2, int2 *__restrict__ dst, bool vec_in) {
+                     int C, uint32_t *__restrict__ cfill2, int2 *__restrict__ dst, bool vec_in,
+                     uint64_t timeout_ns, unsigned *fault) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int W = 1 << fine_log;
   int32_t *win = reinterpret_cast<int32_t *>(smem);
@@ -961,18 +962,23 @@ __global__ void __launch_bounds__(kThreads)
   uint32_t *soff = scnt + C;
   uint32_t *sgb = soff + C;
   __shared__ uint32_t s_warp[16];
+  __shared__ alignas(8) uint64_t bar;
   const int f = blockIdx.x, t = threadIdx.x;
   const int64_t base = static_cast<int64_t>(f) << fine_log;
   const int len = static_cast<int>(min64(W, n - base));
   const int64_t lo = start[f], hi = start[f + 1];
   if (lo >= hi) return;  // block-uniform
-  if (vec_in) {
-    const int4 *s4 = reinterpret_cast<const int4 *>(in + base);
-    for (int q = t; q < (len >> 2); q += kThreads) reinterpret_cast<int4 *>(win)[q] = __ldcs(s4 + q);
-    for (int e = (len & ~3) + t; e < len; e += kThreads) win[e] = in[base + e];
-  } else {
-    for (int e = t; e < len; e += kThreads) win[e] = in[base + e];
+  // the window by one bulk copy (16-byte multiple), the rest by plain loads
+  const uint32_t bulk = vec_in ? (static_cast<uint32_t>(len) * 4u) & ~15u : 0u;
+  if (t == 0 && bulk) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+    mbar_arrive_expect_tx(&bar, bulk);
+    tma_load_1d(win, in + base, bulk, &bar);
   }
+  for (int e = static_cast<int>(bulk / 4) + t; e < len; e += kThreads) win[e] = in[base + e];
+  __syncthreads();  // barrier initialised before anyone waits on it
+  if (bulk && __syncthreads_or(!mbar_wait_bounded(&bar, 0, timeout_ns, fault))) return;
   const unsigned lt = lanemask_lt();
   for (int64_t c0 = lo; c0 < hi; c0 += kTile) {
     for (int i = t; i < C; i += kThreads) scnt[i] = 0;
@@ -1097,7 +1103,7 @@ int tiled_run(const int32_t *in, int32_t *out, int64_t n, const int32_t *loc, in
         pb, start, nullptr, p.fine_log, n, out, aligned16(out));
   } else {
     win_fetch_kernel<<<static_cast<unsigned>(p.F), kThreads, fetch_smem(p.fine_log, p.C), st>>>(
-        pb, start, in, n, p.fine_log, p.coarse_log, p.C, cfill2, pa, vec_in);
+        pb, start, in, n, p.fine_log, p.coarse_log, p.C, cfill2, pa, vec_in, kDefaultWaitNs, fault);
     const int64_t rtiles = static_cast<int64_t>(p.C) << (p.coarse_log - 12);
     win_refine_kernel<<<static_cast<unsigned>(min64(rtiles, rblocks)), kThreads, refine_smem(), st>>>(
         pa, nullptr, cfill2, p.coarse_log, p.fine_log, rtiles, fill2, pb, kDefaultWaitNs, fault);
