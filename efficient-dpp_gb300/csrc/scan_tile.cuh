@@ -174,11 +174,13 @@ template <typename T, int THREADS, int CHUNKS> struct TileScan {
   static constexpr int E = Chunk<T>::E;
   static constexpr int WARPS = THREADS / 32;
   static constexpr int kTile = THREADS * CHUNKS * E;
-  static_assert(WARPS * CHUNKS == 32, "one warp scans the warp totals");
+  static constexpr int NT = WARPS * CHUNKS;  // warp totals of a tile
+  static constexpr int PER = NT / 32;        // warp totals per lane of warp 0
+  static_assert(NT == 32 || NT == 64, "one warp scans the warp totals");
 
   struct Shared {
-    T warp_tot[32];  // [k*WARPS + w] inclusive total of warp w in row k
-    T warp_pre[32];  // exclusive tile prefix of (row k, warp w)
+    T warp_tot[NT];  // [k*WARPS + w] inclusive total of warp w in row k
+    T warp_pre[NT];  // exclusive tile prefix of (row k, warp w)
     T prefix;        // exclusive prefix of the whole tile
     T total;         // tile aggregate
   };
@@ -213,13 +215,24 @@ template <typename T, int THREADS, int CHUNKS> struct TileScan {
     }
   }
 
-  // Phase 2 (warp 0 only, after the barrier): scan the 32 warp totals.
-  // Returns the tile aggregate in every lane of warp 0.
+  // Phase 2 (warp 0 only, after the barrier): scan the NT warp totals, PER
+  // consecutive ones per lane.  Returns the tile aggregate in every lane.
   __device__ __forceinline__ static T phase2_warp0(Shared &sh, int lane) {
-    const T x = sh.warp_tot[lane];
-    const T xi = warp_incl_scan(x, lane);
+    T x[PER];
+    T s = zero_of<T>();
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+      x[i] = sh.warp_tot[lane * PER + i];
+      s = op_add(s, x[i]);
+    }
+    const T xi = warp_incl_scan(s, lane);
     const T ex = shfl_up(xi, 1);
-    sh.warp_pre[lane] = lane == 0 ? zero_of<T>() : ex;
+    T run = lane == 0 ? zero_of<T>() : ex;
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+      sh.warp_pre[lane * PER + i] = run;
+      run = op_add(run, x[i]);
+    }
     return shfl_idx(xi, 31);
   }
 
