@@ -11,9 +11,14 @@ bytes: gather / scatter 12 B per element per call (read index, read
 payload, write payload), independent of the pass count; copy / scale 8 B,
 add / triad 12 B per element.
 
+Schedule: gather / scatter run the shared-memory-window form by default
+(--method tiled; "partition" = L2 windows, "sweep" = the reference's pass-by-
+pass schedule); results are identical for every pass count and schedule.
+
 value     device-timed, inputs resident in HBM (CUDA events, max over ranks)
 e2e       same metric through the C ABI with host buffers: every step copies
-          its inputs from pinned host memory and every output back
+          its inputs from pinned host memory and every output back, the
+          copies on two copy streams overlapping the calls
 roofline  the dominant call of the step against the measured HBM copy rate
 cpu_baseline  the reference's CPU path (OpenMP ports, oracle/) on the host
           cores, on a bounded sample; rank 0 at N=1 only
@@ -64,7 +69,7 @@ def call_bytes(name, n):
     return n * (GS_BYTES if name in ("gather", "scatter") else STREAM_BYTES[name])
 
 
-def call_launches(name, p, method="partition"):
+def call_launches(name, p, method="tiled"):
     """Kernels of this library one call launches."""
     if name not in ("gather", "scatter"):
         return 1
@@ -730,7 +735,7 @@ def main(argv=None):
     ap.add_argument("--cpu-sample", type=int, default=1 << 26)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--method", default="partition", choices=["partition", "sweep", "tiled"],
+    ap.add_argument("--method", default="tiled", choices=["partition", "sweep", "tiled"],
                     help="gather/scatter schedule of the timed step")
     ap.add_argument("--no-compare", action="store_true",
                     help="skip timing the other gather/scatter schedule")
@@ -857,15 +862,22 @@ def main(argv=None):
     # The dominant call of the step: its algorithmic bytes over its CUDA-event
     # duration (all launches of the call, which run back to back on the stream).
     achieved = call_bytes(dom[0], n) / (per_call_ms[dom] * 1e-3) / 1e9
+    # DRAM bytes of one such call from an ncu capture of the tiled schedule
+    # (profiles/traffic.json); the rate they imply shows how close the call's
+    # kernels run to the HBM roofline on the bytes they must move.
     traffic = None
     tf = ROOT / "profiles" / "traffic.json"
-    if tf.exists():
+    if tf.exists() and args.method == "tiled" and n == 1 << 28:
         try:
             traffic = json.loads(tf.read_text()).get(dom_name)
         except Exception:
             traffic = None
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic,
+                "traffic_gbs": None if traffic is None else
+                round(traffic / (per_call_ms[dom] * 1e-3) / 1e9, 1),
+                "traffic_frac": None if traffic is None else
+                round(traffic / (per_call_ms[dom] * 1e-3) / 1e9 / peak, 4),
                 "kernel": dom_name,
                 "launches_per_call": call_launches(dom[0], dom[1], args.method),
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"
