@@ -62,10 +62,12 @@ __device__ __forceinline__ int rank_in_window(int w, uint32_t *scnt, unsigned) {
 }
 
 // Block-wide exclusive scan of scnt[0..nwin) into soff[], returns total.
+// NT threads in the block; s_warp holds NT/32 + 1 entries.
+template <int NT = kThreads>
 __device__ __forceinline__ uint32_t block_scan_counts(const uint32_t *scnt, uint32_t *soff, int nwin,
                                                       uint32_t *s_warp) {
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  const int per = (nwin + kThreads - 1) / kThreads;
+  const int per = (nwin + NT - 1) / NT;
   const int lo = min(nwin, tid * per), hi = min(nwin, lo + per);
   uint32_t s = 0;
   for (int i = lo; i < hi; ++i) s += scnt[i];
@@ -78,15 +80,15 @@ __device__ __forceinline__ uint32_t block_scan_counts(const uint32_t *scnt, uint
   if (lane == 31) s_warp[wid] = incl;
   __syncthreads();
   if (wid == 0) {
-    const uint32_t x = lane < kThreads / 32 ? s_warp[lane] : 0u;
+    const uint32_t x = lane < NT / 32 ? s_warp[lane] : 0u;
     uint32_t xi = x;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
       const uint32_t y = __shfl_up_sync(0xffffffffu, xi, d);
       if (lane >= d) xi += y;
     }
-    if (lane < kThreads / 32) s_warp[lane] = xi - x;
-    if (lane == 31) s_warp[8] = xi;  // total (kThreads / 32 == 8 warps)
+    if (lane < NT / 32) s_warp[lane] = xi - x;
+    if (lane == 31) s_warp[NT / 32] = xi;  // total
   }
   __syncthreads();
   uint32_t run = s_warp[wid] + (incl - s);
@@ -94,7 +96,7 @@ __device__ __forceinline__ uint32_t block_scan_counts(const uint32_t *scnt, uint
     soff[i] = run;
     run += scnt[i];
   }
-  const uint32_t total = s_warp[8];
+  const uint32_t total = s_warp[NT / 32];
   __syncthreads();
   return total;
 }
@@ -164,23 +166,24 @@ __global__ void __launch_bounds__(kThreads)
 // Group the block's pairs by window and append one run per window at the
 // window's global cursor.  pair.x determines the window (x >> log_w); w[e] is
 // -1 for dropped elements; rank[e] from rank_in_window.
-template <int PER>
+template <int PER, int NT = kThreads>
 __device__ __forceinline__ void flush_runs(const int2 (&pr)[PER], const int (&w)[PER],
                                            const int (&rank)[PER], int nwin, int log_w,
                                            uint32_t *scnt, uint32_t *soff, uint32_t *sgb,
                                            uint32_t *s_warp, int2 *stage, uint32_t *fill,
                                            int2 *__restrict__ dst) {
-  const uint32_t total = block_scan_counts(scnt, soff, nwin, s_warp);
-  for (int i = threadIdx.x; i < nwin; i += kThreads)
-    if (scnt[i]) sgb[i] = atomicAdd(&fill[i], scnt[i]);
+  const uint32_t total = block_scan_counts<NT>(scnt, soff, nwin, s_warp);
+  // sgb[w]: global index of the window's run minus its staging offset
+  // (modulo 2^32), so a staged slot s maps to dst[sgb[w] + s]
+  for (int i = threadIdx.x; i < nwin; i += NT)
+    if (scnt[i]) sgb[i] = atomicAdd(&fill[i], scnt[i]) - soff[i];
 #pragma unroll
   for (int e = 0; e < PER; ++e)
     if (w[e] >= 0) stage[soff[w[e]] + rank[e]] = pr[e];
   __syncthreads();
-  for (uint32_t s = threadIdx.x; s < total; s += kThreads) {
+  for (uint32_t s = threadIdx.x; s < total; s += NT) {
     const int2 p = stage[s];
-    const int ww = p.x >> log_w;
-    dst[sgb[ww] + (s - soff[ww])] = p;
+    dst[sgb[p.x >> log_w] + s] = p;
   }
 }
 
@@ -851,16 +854,15 @@ __global__ void __launch_bounds__(kThreads, kRefineBlocksPerSm)
         }
         __syncthreads();
         const uint32_t total = block_scan_counts(scnt, soff, span, s_warp);
-        for (int i = t; i < span; i += kThreads)
-          if (scnt[i]) sgb[i] = atomicAdd(&fill[wlo + i], scnt[i]);
+        for (int i = t; i < span; i += kThreads)  // run start minus staging offset
+          if (scnt[i]) sgb[i] = atomicAdd(&fill[wlo + i], scnt[i]) - soff[i];
 #pragma unroll
         for (int e = 0; e < kPer; ++e)
           if (fid[e] >= 0) buf[soff[fid[e]] + rank[e]] = pr[e];
         __syncthreads();
         for (uint32_t q = t; q < total; q += kThreads) {
           const int2 p = buf[q];
-          const int ww = (p.x >> fine_log) - wlo;
-          dst[sgb[ww] + (q - soff[ww])] = p;
+          dst[sgb[(p.x >> fine_log) - wlo] + q] = p;
         }
       }
       fence_proxy_async_smem();  // generic accesses of buf before the next bulk copy into it
@@ -949,7 +951,10 @@ __global__ void __launch_bounds__(kWinThreads)
 // Gather fetch: one block per fine window f of in[]; the window is loaded
 // once into shared memory, and each pair {loc, i} of the window becomes
 // {i, in[loc]}, appended to the coarse window of i (cursors cfill2).
-__global__ void __launch_bounds__(kThreads)
+constexpr int kFetchThreads = 512;
+constexpr int kFetchPer = kTile / kFetchThreads;  // 8 pairs per thread per sub-tile
+
+__global__ void __launch_bounds__(kFetchThreads)
     win_fetch_kernel(const int2 *__restrict__ pairs, const uint32_t *__restrict__ start,
                      const int32_t *__restrict__ in, int64_t n, int fine_log, int coarse_log,
                      int C, uint32_t *__restrict__ cfill2, int2 *__restrict__ dst, bool vec_in,
@@ -961,7 +966,7 @@ __global__ void __launch_bounds__(kThreads)
   uint32_t *scnt = reinterpret_cast<uint32_t *>(stage + kTile);
   uint32_t *soff = scnt + C;
   uint32_t *sgb = soff + C;
-  __shared__ uint32_t s_warp[16];
+  __shared__ uint32_t s_warp[kFetchThreads / 32 + 1];
   __shared__ alignas(8) uint64_t bar;
   const int f = blockIdx.x, t = threadIdx.x;
   const int64_t base = static_cast<int64_t>(f) << fine_log;
@@ -976,18 +981,18 @@ __global__ void __launch_bounds__(kThreads)
     mbar_arrive_expect_tx(&bar, bulk);
     tma_load_1d(win, in + base, bulk, &bar);
   }
-  for (int e = static_cast<int>(bulk / 4) + t; e < len; e += kThreads) win[e] = in[base + e];
+  for (int e = static_cast<int>(bulk / 4) + t; e < len; e += kFetchThreads) win[e] = in[base + e];
   __syncthreads();  // barrier initialised before anyone waits on it
   if (bulk && __syncthreads_or(!mbar_wait_bounded(&bar, 0, timeout_ns, fault))) return;
   const unsigned lt = lanemask_lt();
   for (int64_t c0 = lo; c0 < hi; c0 += kTile) {
-    for (int i = t; i < C; i += kThreads) scnt[i] = 0;
+    for (int i = t; i < C; i += kFetchThreads) scnt[i] = 0;
     __syncthreads();  // also: window loaded, previous tile's stage consumed
-    int2 pr[kPer];
-    int w[kPer], rank[kPer];
+    int2 pr[kFetchPer];
+    int w[kFetchPer], rank[kFetchPer];
 #pragma unroll
-    for (int e = 0; e < kPer; ++e) {
-      const int64_t j = c0 + static_cast<int64_t>(e) * kThreads + t;
+    for (int e = 0; e < kFetchPer; ++e) {
+      const int64_t j = c0 + static_cast<int64_t>(e) * kFetchThreads + t;
       const bool valid = j < hi;
       const int2 a = valid ? pairs[j] : make_int2(0, 0);
       pr[e] = make_int2(a.y, valid ? win[a.x - base] : 0);  // {i, value}
@@ -995,7 +1000,8 @@ __global__ void __launch_bounds__(kThreads)
       rank[e] = rank_in_window(w[e], scnt, lt);
     }
     __syncthreads();
-    flush_runs<kPer>(pr, w, rank, C, coarse_log, scnt, soff, sgb, s_warp, stage, cfill2, dst);
+    flush_runs<kFetchPer, kFetchThreads>(pr, w, rank, C, coarse_log, scnt, soff, sgb, s_warp, stage,
+                                         cfill2, dst);
     __syncthreads();
   }
 }
@@ -1102,7 +1108,7 @@ int tiled_run(const int32_t *in, int32_t *out, int64_t n, const int32_t *loc, in
     win_apply_kernel<<<static_cast<unsigned>(p.F), kWinThreads, apply_smem(p.fine_log), st>>>(
         pb, start, nullptr, p.fine_log, n, out, aligned16(out));
   } else {
-    win_fetch_kernel<<<static_cast<unsigned>(p.F), kThreads, fetch_smem(p.fine_log, p.C), st>>>(
+    win_fetch_kernel<<<static_cast<unsigned>(p.F), kFetchThreads, fetch_smem(p.fine_log, p.C), st>>>(
         pb, start, in, n, p.fine_log, p.coarse_log, p.C, cfill2, pa, vec_in, kDefaultWaitNs, fault);
     const int64_t rtiles = static_cast<int64_t>(p.C) << (p.coarse_log - 12);
     win_refine_kernel<<<static_cast<unsigned>(min64(rtiles, rblocks)), kThreads, refine_smem(), st>>>(
