@@ -67,23 +67,23 @@ double split_any(const int *d_in, int *d_out, int *d_start, int length, int buck
 
 }  // namespace
 
-// Multi-pass gather / scatter through the partitioned form (same results as
-// the reference's pass-by-pass sweeps, pass windows realised as partitions).
+// Multi-pass gather / scatter through the shared-memory-window form: the same
+// results as the reference's pass-by-pass sweeps for every pass count.
 double gather(const int *d_in, int *d_out, int length, const int *d_loc, int, int, int pass) {
   if (pass < 1) return -1;
-  Temp ws(edpp_gather_workspace_size(length, pass));
+  Temp ws(edpp_gather_tiled_workspace_size(length));
   if (!ws.ok()) return -1;
   return timed([&] {
-    return edpp_gather_i32_ws(d_in, d_out, length, d_loc, pass, ws.p, ws.bytes, nullptr);
+    return edpp_gather_i32_tiled(d_in, d_out, length, d_loc, pass, ws.p, ws.bytes, nullptr);
   });
 }
 
 double scatter(const int *d_in, int *d_out, int length, const int *d_loc, int, int, int pass) {
   if (pass < 1) return -1;
-  Temp ws(edpp_scatter_workspace_size(length, pass));
+  Temp ws(edpp_scatter_tiled_workspace_size(length));
   if (!ws.ok()) return -1;
   return timed([&] {
-    return edpp_scatter_i32_ws(d_in, d_out, length, d_loc, pass, ws.p, ws.bytes, nullptr);
+    return edpp_scatter_i32_tiled(d_in, d_out, length, d_loc, pass, ws.p, ws.bytes, nullptr);
   });
 }
 
