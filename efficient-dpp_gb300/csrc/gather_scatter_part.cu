@@ -174,12 +174,18 @@ __device__ __forceinline__ void flush_runs(const int2 (&pr)[PER], const int (&w)
                                            int2 *__restrict__ dst) {
   const uint32_t total = block_scan_counts<NT>(scnt, soff, nwin, s_warp);
   // sgb[w]: global index of the window's run minus its staging offset
-  // (modulo 2^32), so a staged slot s maps to dst[sgb[w] + s]
-  for (int i = threadIdx.x; i < nwin; i += NT)
+  // (modulo 2^32), so a staged slot s maps to dst[sgb[w] + s].  The first
+  // claim of each thread is consumed only after the staging writes, so its
+  // round trip to L2 overlaps them.
+  const int i0 = threadIdx.x;
+  const uint32_t c0 = i0 < nwin ? scnt[i0] : 0u;
+  const uint32_t g0 = c0 ? atomicAdd(&fill[i0], c0) : 0u;
+  for (int i = i0 + NT; i < nwin; i += NT)
     if (scnt[i]) sgb[i] = atomicAdd(&fill[i], scnt[i]) - soff[i];
 #pragma unroll
   for (int e = 0; e < PER; ++e)
     if (w[e] >= 0) stage[soff[w[e]] + rank[e]] = pr[e];
+  if (c0) sgb[i0] = g0 - soff[i0];
   __syncthreads();
   for (uint32_t s = threadIdx.x; s < total; s += NT) {
     const int2 p = stage[s];
@@ -854,11 +860,16 @@ __global__ void __launch_bounds__(kThreads, kRefineBlocksPerSm)
         }
         __syncthreads();
         const uint32_t total = block_scan_counts(scnt, soff, span, s_warp);
-        for (int i = t; i < span; i += kThreads)  // run start minus staging offset
+        // run start minus staging offset; the first claim's round trip
+        // overlaps the staging writes
+        const uint32_t c0 = t < span ? scnt[t] : 0u;
+        const uint32_t g0 = c0 ? atomicAdd(&fill[wlo + t], c0) : 0u;
+        for (int i = t + kThreads; i < span; i += kThreads)
           if (scnt[i]) sgb[i] = atomicAdd(&fill[wlo + i], scnt[i]) - soff[i];
 #pragma unroll
         for (int e = 0; e < kPer; ++e)
           if (fid[e] >= 0) buf[soff[fid[e]] + rank[e]] = pr[e];
+        if (c0) sgb[t] = g0 - soff[t];
         __syncthreads();
         for (uint32_t q = t; q < total; q += kThreads) {
           const int2 p = buf[q];
