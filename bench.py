@@ -595,6 +595,52 @@ def run_split_workload(args, rank, world):
     return 0
 
 
+def run_radix_workload(args, rank, world):
+    """LSD radix sort on the stable split (8-bit digits): 2^k uniform int32 keys
+    (seed 3), keys only and with int32 values, against torch.sort(stable=True)
+    on the same data (CUB's radix sort, the comparison of
+    obsolete/CUDA/radixSortCUB.cu).  torch orders signed keys; the split sorts
+    the bit pattern, so keys are drawn from [0, 2^31) where both agree."""
+    import torch
+
+    import edpp
+    edpp.lib()
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.set_device(dev)
+    peak, peak_kind = measured_peak_gbs()
+    n = 1 << args.radix_log2n
+    keys = torch.from_numpy(edpp.gen_keys_uniform(n, 3)).to(dev)
+    vals = torch.arange(n, dtype=torch.int32, device=dev)
+    ko = torch.empty_like(keys)
+    vo = torch.empty_like(vals)
+    rows = []
+    for with_vals in (False, True):
+        ws = edpp.workspace(edpp.lib().edpp_radix_sort_workspace_size(n, int(with_vals)), dev)
+        ms = _event_ms(lambda: edpp.radix_sort(keys, vals if with_vals else None, 0, 31, ko,
+                                               vo if with_vals else None, ws),
+                       args.steps, args.warmup)
+        ms_t = _event_ms(lambda: torch.sort(keys, stable=True), args.steps, args.warmup)
+        ref_k, ref_i = torch.sort(keys, stable=True)
+        ok = bool(torch.equal(ko, ref_k)) and (not with_vals or bool(torch.equal(vo, ref_i.int())))
+        rows.append({"values": with_vals, "ms": round(ms, 4), "Mkeys/s": round(n / ms / 1e3, 1),
+                     "torch_sort_ms": round(ms_t, 4), "identical_to_torch": ok})
+        del ws
+    if edpp.sync_status() != edpp.EDPP_OK:
+        raise SystemExit("device fault in the radix workload")
+    head = rows[1]
+    if rank == 0:
+        print(json.dumps({"metric": METRIC, "workload_metric": "radix sort Mkeys/s (31-bit keys, 4 passes)",
+                          "value": head["Mkeys/s"], "unit": "Mkeys/s", "n_gpus": world,
+                          "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["ms"],
+                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                          "dtype": "int32", "data": "synthetic", "peak": peak,
+                          "peak_source": peak_kind,
+                          "config": {"workload": f"radix sort 2^{args.radix_log2n} uniform keys "
+                                                 "[0,2^31), seed 3, bits 0..31"},
+                          "rows": rows}), flush=True)
+    return 0
+
+
 def run_join_workload(args, rank, world):
     """Hash join match count, partitioned (split both sides, shared-memory
     table per partition) and non-partitioned (one device table), |R| = 2^k
@@ -740,7 +786,8 @@ def main(argv=None):
     ap.add_argument("--no-compare", action="store_true",
                     help="skip timing the other gather/scatter schedule")
     ap.add_argument("--workload", default="gs_stream",
-                    choices=["gs_stream", "batch", "serve", "scan", "split", "join", "access"],
+                    choices=["gs_stream", "batch", "serve", "scan", "split", "join", "access",
+                             "radix"],
                     help="gs_stream: multi-pass gather/scatter + STREAM (default); "
                          "batch: 4096 uneven segments, batched vs plain; "
                          "serve: Poisson request stream through the server")
@@ -755,6 +802,7 @@ def main(argv=None):
     ap.add_argument("--split-log2n", type=int, default=28)
     ap.add_argument("--split-buckets", default="", help="split: comma list (default 2..1024)")
     ap.add_argument("--join-log2n", type=int, default=26)
+    ap.add_argument("--radix-log2n", type=int, default=28)
     ap.add_argument("--access-wg-log2n", type=int, default=26)
     ap.add_argument("--scan-config1-only", action="store_true",
                     help="scan: only the config-1 rows")
@@ -776,6 +824,8 @@ def main(argv=None):
         return run_split_workload(args, rank, world)
     if args.workload == "join":
         return run_join_workload(args, rank, world)
+    if args.workload == "radix":
+        return run_radix_workload(args, rank, world)
     if args.workload == "access":
         return run_access_workload(args, rank, world)
 

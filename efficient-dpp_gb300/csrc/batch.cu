@@ -63,6 +63,7 @@ union __align__(128) BatchSmem {
     uint16_t cnt16[kWarps * kMaxB];
     int32_t toff[kMaxB];
     int32_t gofs[kMaxB];
+    uint8_t last[kWarps * kMaxB];  // leader lane per (warp, bucket)
   } split;
   struct {
     uint32_t cnt[kMaxB];
@@ -272,8 +273,15 @@ __global__ void __launch_bounds__(kThreads)
           const int32_t key = valid ? sm.split.keys[pos] : 0;
           const int32_t val = valid ? sm.split.vals[pos] : 0;
           const int b = valid ? static_cast<int>(static_cast<unsigned>(key) & mask) : -1;
-          const unsigned peers =
-              match_low_bits(static_cast<unsigned>(b), kbits, __ballot_sync(0xffffffffu, valid));
+          const unsigned vmask = __ballot_sync(0xffffffffu, valid);
+          unsigned peers;
+          if (kbits <= 5) {
+            peers = match_low_bits(static_cast<unsigned>(b), kbits, vmask);
+          } else {  // one leader lane per bucket, 5 votes on its lane number
+            if (valid) sm.split.last[w * B + b] = static_cast<uint8_t>(lane);
+            __syncwarp();
+            peers = match_low_bits(valid ? sm.split.last[w * B + b] : 0u, 5, vmask);
+          }
           const unsigned lower = peers & lt;
           const uint16_t before = valid ? my[b] : 0;
           __syncwarp();

@@ -111,7 +111,8 @@ template <int THREADS> struct ScatterCfg {
 template <int THREADS, int LAYOUT> size_t scatter_smem_bytes(int buckets) {
   const size_t stage = (LAYOUT == EDPP_KO) ? kTile * 4 : kTile * 8;
   return stage + round_up(static_cast<size_t>(ScatterCfg<THREADS>::kWarps) * buckets * 2, 16) +
-         2 * static_cast<size_t>(buckets) * 4;
+         2 * static_cast<size_t>(buckets) * 4 +
+         static_cast<size_t>(ScatterCfg<THREADS>::kWarps) * buckets;  // leader bytes
 }
 
 template <int THREADS, int LAYOUT>
@@ -133,6 +134,7 @@ __global__ void __launch_bounds__(THREADS)
   int32_t *toff = reinterpret_cast<int32_t *>(
       smem + stage + round_up(static_cast<size_t>(C::kWarps) * buckets * 2, 16));
   int32_t *gofs = toff + buckets;
+  uint8_t *s_last = reinterpret_cast<uint8_t *>(gofs + buckets);  // [kWarps][buckets]
   __shared__ alignas(8) uint64_t bar;
 
   const int64_t t = blockIdx.x;
@@ -180,6 +182,7 @@ __global__ void __launch_bounds__(THREADS)
   const unsigned lt = lanemask_lt();
   const int kbits = 31 - __clz(buckets);
   uint16_t *my_cnt = cnt16 + w * buckets;
+  uint8_t *my_last = s_last + w * buckets;
   int32_t kk[C::kIters];
   int32_t vv[C::kIters];
   uint32_t rk[(C::kIters + 1) / 2];  // two 16-bit ranks per register
@@ -199,7 +202,18 @@ __global__ void __launch_bounds__(THREADS)
       }
     }
     const int b = valid ? static_cast<int>((static_cast<unsigned>(key) >> shift) & mask) : -1;
-    const unsigned peers = match_low_bits(static_cast<unsigned>(b), kbits, __ballot_sync(0xffffffffu, valid));
+    const unsigned vmask = __ballot_sync(0xffffffffu, valid);
+    unsigned peers;
+    if (kbits <= 5) {
+      peers = match_low_bits(static_cast<unsigned>(b), kbits, vmask);
+    } else {
+      // more than 5 bucket bits: the lanes of a bucket agree on one leader
+      // lane (whichever write lands), and 5 votes on the leader's lane
+      // number find the group
+      if (valid) my_last[b] = static_cast<uint8_t>(lane);
+      __syncwarp();
+      peers = match_low_bits(valid ? my_last[b] : 0u, 5, vmask);
+    }
     const unsigned lower = peers & lt;
     const uint16_t before = valid ? my_cnt[b] : 0;
     __syncwarp();
@@ -313,7 +327,8 @@ template <int THREADS, int LAYOUT> int set_smem_attr() {
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64) dev = 0;
   std::call_once(once[dev], [&] {
-    const size_t bytes = scatter_smem_bytes<THREADS, LAYOUT>(kMaxBuckets);
+    // 512 threads serve up to 1024 buckets, 256 threads the rest
+    const size_t bytes = scatter_smem_bytes<THREADS, LAYOUT>(THREADS == 512 ? 1024 : kMaxBuckets);
     status[dev] = cuda_status(cudaFuncSetAttribute(split_scatter_kernel<THREADS, LAYOUT>,
                                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                    static_cast<int>(bytes)));
