@@ -254,6 +254,11 @@ def ref_cuda():
         L.refcu_gather_scatter.argtypes = [_I, _VP, _VP, _VP, ctypes.c_longlong]
         L.refcu_stream_i32.argtypes = [_I, _VP, _VP, _VP, ctypes.c_longlong]
         L.refcu_cub_exclusive_sum_i32.argtypes = [_VP, _VP, ctypes.c_longlong]
+        FP = ctypes.POINTER(ctypes.c_float)
+        L.refcu_time_gather_scatter.argtypes = [_I, _VP, ctypes.c_longlong, _I, FP]
+        L.refcu_time_cub_scan.argtypes = [ctypes.c_longlong, _I, FP]
+        L.refcu_time_split.argtypes = [_VP, ctypes.c_longlong, _I, _I, FP]
+        L.refcu_time_stream_i32.argtypes = [_I, ctypes.c_longlong, _I, FP]
         rc = L.refcu_init(str(HERE / "_ref").encode())
         if rc != 0:
             return None
