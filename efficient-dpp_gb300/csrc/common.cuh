@@ -192,6 +192,9 @@ inline int launch_status() { return cuda_status(cudaGetLastError()); }
 // SM count of the current device (cached per device).
 int device_sm_count();
 
+// L2 size of the current device in bytes (cached).
+int device_l2_bytes();
+
 // Device address of the fault word of the current device (cached).
 unsigned *fault_word();
 

@@ -111,12 +111,10 @@ __global__ void __launch_bounds__(kLbThreads, sizeof(T) == 4 ? 12 : 8)
 
 // ---- RTS / SSA building blocks ----------------------------------------------
 
-// Per-block sum of the block's contiguous range [b*per, min((b+1)*per, n)).
+// Sum of in[lo, hi) by the whole block; the result is valid in thread 0.
+// lo is a multiple of the tile size (16-byte aligned when vec).
 template <typename T>
-__global__ void __launch_bounds__(kThreads)
-    reduce_blocks_kernel(const T *in, int64_t n, int64_t per, T *partials, bool vec) {
-  const int64_t lo = static_cast<int64_t>(blockIdx.x) * per;
-  const int64_t hi = min64(n, lo + per);
+__device__ __forceinline__ T block_reduce_range(const T *in, int64_t lo, int64_t hi, bool vec) {
   T acc = zero_of<T>();
   if (lo < hi) {
     constexpr int E = Chunk<T>::E;
@@ -148,11 +146,22 @@ __global__ void __launch_bounds__(kThreads)
   acc = warp_sum(acc);
   if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = acc;
   __syncthreads();
+  T v = zero_of<T>();
   if (threadIdx.x < 32) {
-    T v = threadIdx.x < kThreads / 32 ? ws[threadIdx.x] : zero_of<T>();
+    v = threadIdx.x < kThreads / 32 ? ws[threadIdx.x] : zero_of<T>();
     v = warp_sum(v);
-    if (threadIdx.x == 0) partials[blockIdx.x] = v;
   }
+  return v;
+}
+
+// Per-block sum of the block's contiguous range [b*per, min((b+1)*per, n)).
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+    reduce_blocks_kernel(const T *in, int64_t n, int64_t per, T *partials, bool vec) {
+  const int64_t lo = static_cast<int64_t>(blockIdx.x) * per;
+  const int64_t hi = min64(n, lo + per);
+  const T v = block_reduce_range(in, lo, hi, vec);
+  if (threadIdx.x == 0) partials[blockIdx.x] = v;
 }
 
 // Exclusive scan of `m` partial sums in place, one block of 1024 threads.
@@ -186,30 +195,16 @@ template <typename T> __global__ void __launch_bounds__(1024) scan_partials_kern
 // `offsets[b]` (RTS) or 0 (SSA, which then records its block total in
 // totals[b]).  Tiles are double-buffered: the bulk copy of tile i+1 is in
 // flight while tile i is scanned.
-template <typename T, bool kInclusive, bool kFromOffsets>
-__global__ void __launch_bounds__(kThreads)
-    scan_blocks_kernel(const T *in, T *out, int64_t n, int64_t tpb, const T *offsets, T *totals,
-                       bool tma, bool vec_out, uint64_t timeout_ns, unsigned *fault) {
+// Scan tiles [t_lo, t_hi) in order starting from `running`; returns the
+// running sum after the last tile (false: a bulk copy timed out).  `bar`
+// must be initialised; buffers and barriers are the caller's shared memory.
+template <typename T, bool kInclusive>
+__device__ bool scan_tile_run(const T *in, T *out, int64_t n, int64_t t_lo, int64_t t_hi,
+                              T &running, T (*buf)[TS<T>::kTile], typename TS<T>::Shared &sh,
+                              uint64_t *bar, bool tma, bool vec_out, uint64_t timeout_ns,
+                              unsigned *fault) {
   using S = TS<T>;
   constexpr int kTile = S::kTile;
-  __shared__ alignas(128) T buf[2][kTile];
-  __shared__ typename S::Shared sh;
-  __shared__ alignas(8) uint64_t bar[2];
-
-  const int64_t num_tiles = (n + kTile - 1) / kTile;
-  const int64_t t_lo = static_cast<int64_t>(blockIdx.x) * tpb;
-  const int64_t t_hi = min64(num_tiles, t_lo + tpb);
-  if (threadIdx.x == 0) {
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
-    fence_mbar_init();
-  }
-  __syncthreads();
-  T running = kFromOffsets ? offsets[blockIdx.x] : zero_of<T>();
-  if (t_lo >= t_hi) {
-    if (!kFromOffsets && threadIdx.x == 0) totals[blockIdx.x] = zero_of<T>();
-    return;
-  }
   auto count_of = [&](int64_t t) { return static_cast<int>(min64(kTile, n - t * kTile)); };
   // Prologue: stage the first tile.
   uint32_t bulk_cur = stage_tile<T, kTile, kThreads>(buf[0], in + t_lo * kTile, count_of(t_lo), tma,
@@ -225,7 +220,7 @@ __global__ void __launch_bounds__(kThreads)
       bulk_next = stage_tile<T, kTile, kThreads>(buf[slot ^ 1], in + (t + 1) * kTile,
                                                  count_of(t + 1), tma, &bar[slot ^ 1]);
     if (bulk_cur) {
-      if (!mbar_wait_bounded(&bar[slot], (phase >> slot) & 1u, timeout_ns, fault)) return;
+      if (!mbar_wait_bounded(&bar[slot], (phase >> slot) & 1u, timeout_ns, fault)) return false;
       phase ^= 1u << slot;
     }
     __syncthreads();  // plain-load part of both buffers visible
@@ -244,7 +239,117 @@ __global__ void __launch_bounds__(kThreads)
     bulk_cur = bulk_next;
     __syncthreads();  // everyone done with buf[slot] and sh before reuse
   }
+  return true;
+}
+
+template <typename T, bool kInclusive, bool kFromOffsets>
+__global__ void __launch_bounds__(kThreads)
+    scan_blocks_kernel(const T *in, T *out, int64_t n, int64_t tpb, const T *offsets, T *totals,
+                       bool tma, bool vec_out, uint64_t timeout_ns, unsigned *fault) {
+  using S = TS<T>;
+  constexpr int kTile = S::kTile;
+  __shared__ alignas(128) T buf[2][kTile];
+  __shared__ typename S::Shared sh;
+  __shared__ alignas(8) uint64_t bar[2];
+  const int64_t num_tiles = (n + kTile - 1) / kTile;
+  const int64_t t_lo = static_cast<int64_t>(blockIdx.x) * tpb;
+  const int64_t t_hi = min64(num_tiles, t_lo + tpb);
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  T running = kFromOffsets ? offsets[blockIdx.x] : zero_of<T>();
+  if (t_lo < t_hi &&
+      !scan_tile_run<T, kInclusive>(in, out, n, t_lo, t_hi, running, buf, sh, bar, tma, vec_out,
+                                    timeout_ns, fault))
+    return;
   if (!kFromOffsets && threadIdx.x == 0) totals[blockIdx.x] = running;
+}
+
+// One-launch reduce-then-scan for inputs that fit in L2: every block reduces
+// its run of tiles, the last block to finish scans the block sums, the others
+// wait for it (bounded), and every block then scans its tiles again, now from
+// L2.  Launched cooperatively, so all blocks are resident together.
+template <typename T, bool kInclusive>
+__global__ void __launch_bounds__(kThreads)
+    rts_fused_kernel(const T *in, T *out, int64_t n, int64_t tpb, T *partials, unsigned *ctl,
+                     bool tma, bool vec_out, uint64_t timeout_ns, unsigned *fault) {
+  using S = TS<T>;
+  constexpr int kTile = S::kTile;
+  __shared__ alignas(128) T buf[2][kTile];
+  __shared__ typename S::Shared sh;
+  __shared__ alignas(8) uint64_t bar[2];
+  __shared__ int s_last, s_ok;
+  const int64_t num_tiles = (n + kTile - 1) / kTile;
+  const int64_t t_lo = static_cast<int64_t>(blockIdx.x) * tpb;
+  const int64_t t_hi = min64(num_tiles, t_lo + tpb);
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  // 1. block sum of my tiles
+  const T agg = t_lo < t_hi ? block_reduce_range(in, t_lo * kTile, min64(n, t_hi * kTile), tma)
+                            : zero_of<T>();
+  if (tid == 0) {
+    partials[blockIdx.x] = agg;
+    __threadfence();
+    s_last = atomicAdd(&ctl[0], 1u) + 1u == gridDim.x;
+  }
+  __syncthreads();
+  // 2. the last block scans the block sums (exclusive, in place) and releases the rest
+  if (s_last) {
+    __threadfence();
+    const int m = static_cast<int>(gridDim.x);
+    const int per = (m + kThreads - 1) / kThreads;
+    const int lo = min(m, tid * per), hi = min(m, lo + per);
+    T sum = zero_of<T>();
+    for (int i = lo; i < hi; ++i) sum = op_add(sum, __ldcg(partials + i));
+    __shared__ T wsum[kThreads / 32];
+    const int lane = tid & 31, w = tid >> 5;
+    const T si = warp_incl_scan(sum, lane);
+    if (lane == 31) wsum[w] = si;
+    __syncthreads();
+    if (w == 0) {
+      const T x = lane < kThreads / 32 ? wsum[lane] : zero_of<T>();
+      const T xi = warp_incl_scan(x, lane);
+      const T ex = shfl_up(xi, 1);
+      if (lane < kThreads / 32) wsum[lane] = lane == 0 ? zero_of<T>() : ex;
+    }
+    __syncthreads();
+    const T ex_t = shfl_up(si, 1);
+    T run = op_add(wsum[w], lane == 0 ? zero_of<T>() : ex_t);
+    for (int i = lo; i < hi; ++i) {
+      const T v = __ldcg(partials + i);
+      partials[i] = run;
+      run = op_add(run, v);
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) st_release_u32(&ctl[1], 1u);
+  }
+  // 3. wait for the block offsets (bounded)
+  if (tid == 0) {
+    bool ok = ld_acquire_u32(&ctl[1]) != 0u;
+    if (!ok) {
+      const uint64_t t0 = globaltimer_ns();
+      while (!(ok = ld_acquire_u32(&ctl[1]) != 0u)) {
+        if (globaltimer_ns() - t0 > timeout_ns) break;
+        __nanosleep(64);
+      }
+    }
+    if (!ok) raise_fault(fault, EDPP_FAULT_TIMEOUT);
+    s_ok = ok ? 1 : 0;
+  }
+  __syncthreads();
+  if (!s_ok) return;
+  T running = __ldcg(partials + blockIdx.x);
+  if (t_lo < t_hi)
+    scan_tile_run<T, kInclusive>(in, out, n, t_lo, t_hi, running, buf, sh, bar, tma, vec_out,
+                                 timeout_ns, fault);
 }
 
 // SSA third pass: out[range of block b] += offsets[b].
@@ -342,6 +447,40 @@ int scan_impl(const T *in, T *out, int64_t n, int algo, void *ws, size_t ws_byte
   chunk_grid<T>(n, blocks, tpb);
   T *partials = reinterpret_cast<T *>(w + kHeader);
   const int64_t per = tpb * TS<T>::kTile;
+  if (algo == EDPP_SCAN_RTS &&
+      static_cast<double>(n) * sizeof(T) <= 0.6 * static_cast<double>(device_l2_bytes())) {
+    // the input stays in L2 between the reduce and the scan: one launch
+    static int resident[64];
+    static std::once_flag once[64];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) dev = 0;
+    std::call_once(once[dev], [dev] {
+      int per_sm = 0;
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rts_fused_kernel<T, kInclusive>,
+                                                        kThreads, 0) != cudaSuccess)
+        per_sm = 0;
+      resident[dev] = per_sm * device_sm_count();
+    });
+    if (resident[dev] > 0) {
+      const int64_t tiles = tiles_of<T>(n);
+      const int64_t g0 = std::min<int64_t>({tiles, resident[dev], kMaxChunkBlocks});
+      const int64_t ftpb = (tiles + g0 - 1) / g0;
+      const int64_t g = (tiles + ftpb - 1) / ftpb;
+      if (cudaMemsetAsync(w, 0, kHeader, st) != cudaSuccess) return EDPP_ECUDA;
+      unsigned *ctl = reinterpret_cast<unsigned *>(w);
+      int64_t n_arg = n, tpb_arg = ftpb;
+      bool tma_arg = tma, vec_arg = vec_out;
+      uint64_t to_arg = timeout_ns;
+      void *args[] = {const_cast<T **>(&in), &out, &n_arg, &tpb_arg, &partials, &ctl,
+                      &tma_arg, &vec_arg, &to_arg, &fault};
+      if (cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(rts_fused_kernel<T, kInclusive>),
+                                      dim3(static_cast<unsigned>(g)), dim3(kThreads), args, 0,
+                                      st) != cudaSuccess)
+        return launch_status();
+      return launch_status();
+    }
+  }
   if (algo == EDPP_SCAN_RTS) {
     reduce_blocks_kernel<T><<<static_cast<unsigned>(blocks), kThreads, 0, st>>>(in, n, per,
                                                                                 partials, tma);

@@ -112,7 +112,7 @@ template <int THREADS, int LAYOUT> size_t scatter_smem_bytes(int buckets) {
   const size_t stage = (LAYOUT == EDPP_KO) ? kTile * 4 : kTile * 8;
   return stage + round_up(static_cast<size_t>(ScatterCfg<THREADS>::kWarps) * buckets * 2, 16) +
          2 * static_cast<size_t>(buckets) * 4 +
-         static_cast<size_t>(ScatterCfg<THREADS>::kWarps) * buckets;  // leader bytes
+         static_cast<size_t>(ScatterCfg<THREADS>::kWarps) * std::min(buckets, 256);  // leaders
 }
 
 template <int THREADS, int LAYOUT>
@@ -134,7 +134,7 @@ __global__ void __launch_bounds__(THREADS)
   int32_t *toff = reinterpret_cast<int32_t *>(
       smem + stage + round_up(static_cast<size_t>(C::kWarps) * buckets * 2, 16));
   int32_t *gofs = toff + buckets;
-  uint8_t *s_last = reinterpret_cast<uint8_t *>(gofs + buckets);  // [kWarps][buckets]
+  uint8_t *s_last = reinterpret_cast<uint8_t *>(gofs + buckets);  // [kWarps][min(buckets, 256)]
   __shared__ alignas(8) uint64_t bar;
 
   const int64_t t = blockIdx.x;
@@ -182,7 +182,7 @@ __global__ void __launch_bounds__(THREADS)
   const unsigned lt = lanemask_lt();
   const int kbits = 31 - __clz(buckets);
   uint16_t *my_cnt = cnt16 + w * buckets;
-  uint8_t *my_last = s_last + w * buckets;
+  uint8_t *my_last = s_last + w * min(buckets, 256);
   int32_t kk[C::kIters];
   int32_t vv[C::kIters];
   uint32_t rk[(C::kIters + 1) / 2];  // two 16-bit ranks per register
@@ -207,12 +207,14 @@ __global__ void __launch_bounds__(THREADS)
     if (kbits <= 5) {
       peers = match_low_bits(static_cast<unsigned>(b), kbits, vmask);
     } else {
-      // more than 5 bucket bits: the lanes of a bucket agree on one leader
-      // lane (whichever write lands), and 5 votes on the leader's lane
-      // number find the group
-      if (valid) my_last[b] = static_cast<uint8_t>(lane);
+      // more than 5 bucket bits: the lanes sharing the low 8 bucket bits
+      // agree on one leader lane (whichever write lands), 5 votes on the
+      // leader's lane number find that group, and one vote per bucket bit
+      // above the 8th splits it
+      if (valid) my_last[b & 255] = static_cast<uint8_t>(lane);
       __syncwarp();
-      peers = match_low_bits(valid ? my_last[b] : 0u, 5, vmask);
+      peers = match_low_bits(valid ? my_last[b & 255] : 0u, 5, vmask);
+      if (kbits > 8) peers &= match_low_bits(static_cast<unsigned>(b) >> 8, kbits - 8, vmask);
     }
     const unsigned lower = peers & lt;
     const uint16_t before = valid ? my_cnt[b] : 0;

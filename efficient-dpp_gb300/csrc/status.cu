@@ -13,6 +13,7 @@ namespace {
 constexpr int kMaxDevices = 64;
 std::once_flag g_dev_once[kMaxDevices];
 int g_sm_count[kMaxDevices];
+int g_l2_bytes[kMaxDevices];
 unsigned *g_fault_ptr[kMaxDevices];
 
 int current_device() {
@@ -26,6 +27,10 @@ void init_device(int d) {
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, d) != cudaSuccess || sms <= 0)
     sms = kGb300Sms;
   g_sm_count[d] = sms;
+  int l2 = 0;
+  if (cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, d) != cudaSuccess || l2 <= 0)
+    l2 = 126 << 20;
+  g_l2_bytes[d] = l2;
   void *p = nullptr;
   if (cudaGetSymbolAddress(&p, g_fault_word) != cudaSuccess) p = nullptr;
   g_fault_ptr[d] = static_cast<unsigned *>(p);
@@ -36,6 +41,12 @@ int device_sm_count() {
   const int d = current_device();
   std::call_once(g_dev_once[d], init_device, d);
   return g_sm_count[d];
+}
+
+int device_l2_bytes() {
+  const int d = current_device();
+  std::call_once(g_dev_once[d], init_device, d);
+  return g_l2_bytes[d];
 }
 
 unsigned *fault_word() {
