@@ -1081,11 +1081,6 @@ int tiled_run(const int32_t *in, int32_t *out, int64_t n, const int32_t *loc, in
   if (!in || !out || !loc) return EDPP_EINVAL;
   if (n > INT32_MAX) return EDPP_EINVAL;
   if (!tiled_fits(n)) return part_run<kScatter>(in, out, n, loc, 0, ws, ws_bytes, stream);
-  // A gather whose source is at most ~2.5x L2 keeps enough of it in L2 that
-  // the direct random sweep wins (measured: 2^26 int32 1.0-1.2 ms direct,
-  // 1.36 ms tiled; 2^28 5.6-6.0 ms direct, 5.2-5.3 ms tiled).
-  if (!kScatter && static_cast<double>(n) * 4.0 <= 2.5 * static_cast<double>(device_l2_bytes()))
-    return edpp_gather_i32(in, out, n, loc, 1, stream);
   const TPlan p = tplan(n);
   const TLayout L = tlayout_of(n, p, !kScatter);
   if (!ws || ws_bytes < L.bytes) return EDPP_ENOMEM;
@@ -1180,6 +1175,13 @@ int edpp_gather_i32_tiled(const int32_t *in, int32_t *out, int64_t length, const
 int edpp_scatter_i32_tiled(const int32_t *in, int32_t *out, int64_t length, const int32_t *loc,
                            int pass, void *ws, size_t ws_bytes, void *stream) {
   return edpp::tiled_run<true>(in, out, length, loc, pass, ws, ws_bytes, stream);
+}
+
+int edpp_gather_prefers_direct(int64_t length) {
+  // A gather whose source is at most ~2.5x L2 keeps enough of it in L2 that
+  // the direct random sweep wins (measured: 2^26 int32 1.0-1.2 ms direct,
+  // 1.36 ms tiled; 2^28 5.6-6.0 ms direct, 5.2-5.3 ms tiled).
+  return static_cast<double>(length) * 4.0 <= 2.5 * static_cast<double>(edpp::device_l2_bytes());
 }
 
 }  // extern "C"

@@ -71,6 +71,8 @@ double split_any(const int *d_in, int *d_out, int *d_start, int length, int buck
 // results as the reference's pass-by-pass sweeps for every pass count.
 double gather(const int *d_in, int *d_out, int length, const int *d_loc, int, int, int pass) {
   if (pass < 1) return -1;
+  if (edpp_gather_prefers_direct(length))  // the source stays in L2: one direct sweep
+    return timed([&] { return edpp_gather_i32(d_in, d_out, length, d_loc, 1, nullptr); });
   Temp ws(edpp_gather_tiled_workspace_size(length));
   if (!ws.ok()) return -1;
   return timed([&] {

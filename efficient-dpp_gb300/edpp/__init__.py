@@ -67,6 +67,7 @@ SIGNATURES = {
     "edpp_access_wg_i32": (_I, [_VP, _I64, _VP, _I, _I, _VP, _VP, _VP]),
     "edpp_cache_heat_i32": (_I, [_VP, _I64, _I, _I, _VP]),
     "edpp_local_scan_i32": (_I, [_VP, _VP, _I, _I, _I, _VP]),
+    "edpp_gather_prefers_direct": (_I, [_I64]),
     "edpp_gather_tiled_workspace_size": (_SZ, [_I64]),
     "edpp_scatter_tiled_workspace_size": (_SZ, [_I64]),
     "edpp_gather_i32_tiled": (_I, [_VP, _VP, _I64, _VP, _I, _VP, _SZ, _VP]),
@@ -192,6 +193,10 @@ def _gs(kind, inp, loc, passes, out, method, ws):
     if out is None:
         out = torch.zeros(n, dtype=torch.int32, device=loc.device)
     st = current_stream_handle()
+    if method == "auto":  # the faster schedule for this size
+        method = ("sweep" if kind == "gather" and lib().edpp_gather_prefers_direct(n)
+                  else "tiled")
+        passes = 1 if method == "sweep" else passes
     if method == "sweep":
         f = lib().edpp_gather_i32 if kind == "gather" else lib().edpp_scatter_i32
         check(f(_p(inp), _p(out), n, _p(loc), int(passes), st), kind)
@@ -210,7 +215,7 @@ def _gs(kind, inp, loc, passes, out, method, ws):
 
 
 def gs_workspace_bytes(kind: str, n: int, passes: int, method: str = "partition") -> int:
-    if method == "tiled":
+    if method in ("tiled", "auto"):
         f = (lib().edpp_gather_tiled_workspace_size if kind == "gather"
              else lib().edpp_scatter_tiled_workspace_size)
         return f(int(n))
@@ -224,7 +229,8 @@ def gather(inp, loc, passes: int = 1, out=None, method: str = "sweep", ws=None):
     """out[i] = inp[loc[i]].  method "sweep": one launch per pass window, each
     reading all of loc (the reference's schedule); "partition": the windows
     as partitions (passes=0 sizes them to L2); "tiled": shared-memory
-    windows (the result does not depend on passes)."""
+    windows; "auto": the faster of the single direct sweep and "tiled" for
+    this size (the result does not depend on passes or method)."""
     return _gs("gather", inp, loc, passes, out, method, ws)
 
 

@@ -10,7 +10,7 @@ pytestmark = pytest.mark.gpu
 PASSES = [1, 2, 4, 8, 16]
 
 
-METHODS = ["sweep", "partition", "tiled"]
+METHODS = ["sweep", "partition", "tiled", "auto"]
 
 
 @pytest.mark.parametrize("method", METHODS)
