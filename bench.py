@@ -140,10 +140,20 @@ class ClockSampler:
             self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=self.file, stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
+            return self
+        # let the sampler start before the timed region opens (its first
+        # sample), so that every sample falls inside the timed region's span
+        t0 = time.time()
+        while time.time() - t0 < 3.0 and self.proc.poll() is None:
+            self.file.flush()
+            if os.path.getsize(self.file.name) > 0:
+                break
+            time.sleep(0.02)
+        self.skip = sum(1 for _ in open(self.file.name))
         return self
 
     def __exit__(self, *exc):
@@ -159,7 +169,7 @@ class ClockSampler:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.file.flush()
         rows = []
-        for line in Path(self.file.name).read_text().splitlines():
+        for line in Path(self.file.name).read_text().splitlines()[getattr(self, "skip", 0):]:
             parts = [s.strip() for s in line.split(",")]
             if len(parts) < 9:
                 continue
@@ -773,7 +783,7 @@ def run_access_workload(args, rank, world):
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawTextHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="edpp", choices=["edpp", "reference"])
     ap.add_argument("--log2n", type=int, default=28)
