@@ -127,3 +127,32 @@ def test_against_reference_cub_exclusive_sum(cuda, edpp, orc):
                                               ctypes.c_void_p(ref.ctypes.data), n) == 0
         for algo in ALGOS:
             np.testing.assert_array_equal(to_host(edpp.scan(to_dev(x), algo=algo)), ref)
+
+
+@pytest.mark.parametrize("algo", ALGOS)
+@pytest.mark.parametrize("dt,n", [("int32", (1 << 25) + 3), ("int64", (1 << 24) + 5)])
+def test_beyond_l2_bit_exact(cuda, edpp, orc, algo, dt, n):
+    # larger than 60% of L2: the three-launch RTS/SSA paths and many look-back tiles
+    x = (edpp.gen_uniform_i32(n, 4, -5000, 5000) if dt == "int32"
+         else edpp.gen_uniform_i64(n, 4, -2**40, 2**40))
+    for inclusive in (False, True):
+        y = to_host(edpp.scan(to_dev(x), inclusive=inclusive, algo=algo))
+        np.testing.assert_array_equal(y, orc.scan(x, inclusive=inclusive))
+
+
+@pytest.mark.parametrize("algo", ALGOS)
+def test_config4_full_size_differences(cuda, edpp, algo):
+    # 2^30 int32 in [0,100] (seed 1): consecutive differences of the
+    # exclusive scan give back the input, the inclusive scan is the
+    # exclusive one shifted by the input, and the total matches a
+    # sum in int64 taken modulo 2^32
+    torch = cuda
+    n = 1 << 30
+    x = torch.from_numpy(edpp.gen_uniform_i32(n, 1, 0, 100)).to("cuda")
+    ex = edpp.scan(x, inclusive=False, algo=algo)
+    assert int(ex[0]) == 0
+    assert bool(torch.equal(ex[1:] - ex[:-1], x[:-1]))
+    inc = edpp.scan(x, inclusive=True, algo=algo)
+    assert bool(torch.equal(inc - ex, x))
+    total = int(x.sum(dtype=torch.int64)) & 0xFFFFFFFF
+    assert (int(inc[-1]) & 0xFFFFFFFF) == total
