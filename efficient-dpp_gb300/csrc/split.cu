@@ -186,6 +186,10 @@ __global__ void __launch_bounds__(THREADS)
   int32_t kk[C::kIters];
   int32_t vv[C::kIters];
   uint32_t rk[(C::kIters + 1) / 2];  // two 16-bit ranks per register
+  // Up to 32 buckets: lane L keeps the warp's running count of bucket L in a
+  // register; the per-bit votes give both this lane's group and bucket L's
+  // group, so the loop needs no shared memory and no warp barriers.
+  uint32_t lane_cnt = 0;
 #pragma unroll
   for (int it = 0; it < C::kIters; ++it) {
     const int pos = w * C::kSeg + it * 32 + lane;
@@ -203,10 +207,24 @@ __global__ void __launch_bounds__(THREADS)
     }
     const int b = valid ? static_cast<int>((static_cast<unsigned>(key) >> shift) & mask) : -1;
     const unsigned vmask = __ballot_sync(0xffffffffu, valid);
-    unsigned peers;
     if (kbits <= 5) {
-      peers = match_low_bits(static_cast<unsigned>(b), kbits, vmask);
-    } else {
+      unsigned peers = vmask, mine = vmask;
+      for (int i = 0; i < kbits; ++i) {
+        const unsigned bb = __ballot_sync(0xffffffffu, (b >> i) & 1);
+        peers &= ((b >> i) & 1) ? bb : ~bb;
+        mine &= ((lane >> i) & 1) ? bb : ~bb;  // the lanes holding bucket `lane`
+      }
+      const uint32_t before = __shfl_sync(0xffffffffu, lane_cnt, b & 31);
+      if (lane < buckets) lane_cnt += __popc(mine);
+      kk[it] = key;
+      vv[it] = val;
+      const uint32_t r = valid ? before + __popc(peers & lt) : 0u;
+      if (it & 1) rk[it >> 1] |= r << 16;
+      else rk[it >> 1] = r;
+      continue;
+    }
+    unsigned peers;
+    {
       // more than 5 bucket bits: the lanes sharing the low 8 bucket bits
       // agree on one leader lane (whichever write lands), 5 votes on the
       // leader's lane number find that group, and one vote per bucket bit
@@ -227,6 +245,7 @@ __global__ void __launch_bounds__(THREADS)
     if (it & 1) rk[it >> 1] |= r << 16;
     else rk[it >> 1] = r;
   }
+  if (kbits <= 5 && lane < buckets) my_cnt[lane] = static_cast<uint16_t>(lane_cnt);
   __syncthreads();
 
   // -- per bucket: exclusive prefix over warps, tile count, tile offsets --
