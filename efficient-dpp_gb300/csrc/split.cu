@@ -108,19 +108,15 @@ template <int THREADS> struct ScatterCfg {
 };
 
 // Dynamic shared memory of the scatter kernel.
-template <int THREADS, int LAYOUT, int NBUF = 1> size_t scatter_smem_bytes(int buckets) {
-  const size_t stage = NBUF * ((LAYOUT == EDPP_KO) ? kTile * 4 : kTile * 8);
+template <int THREADS, int LAYOUT> size_t scatter_smem_bytes(int buckets) {
+  const size_t stage = (LAYOUT == EDPP_KO) ? kTile * 4 : kTile * 8;
   return stage + round_up(static_cast<size_t>(ScatterCfg<THREADS>::kWarps) * buckets * 2, 16) +
          2 * static_cast<size_t>(buckets) * 4 +
          static_cast<size_t>(ScatterCfg<THREADS>::kWarps) * std::min(buckets, 256);  // leaders
 }
 
-// NBUF == 1: one block per tile (grid = tiles).  NBUF == 2: persistent
-// blocks take tiles blockIdx, +gridDim, ...; the bulk copy of the tile after
-// next lands in the other staging buffer while this one is ranked, re-laid
-// out and written.
-template <int THREADS, int LAYOUT, int NBUF>
-__global__ void __launch_bounds__(THREADS, 2)
+template <int THREADS, int LAYOUT>
+__global__ void __launch_bounds__(THREADS)
     split_scatter_kernel(const int32_t *__restrict__ keys_in, int32_t *__restrict__ keys_out,
                          const int32_t *__restrict__ vals_in, int32_t *__restrict__ vals_out,
                          int64_t n, int buckets, int shift, int64_t tiles,
@@ -129,60 +125,45 @@ __global__ void __launch_bounds__(THREADS, 2)
   using C = ScatterCfg<THREADS>;
   constexpr bool kKV = LAYOUT != EDPP_KO;
   extern __shared__ __align__(128) unsigned char smem[];
-  // Layout: stage x NBUF (keys[kTile] + vals[kTile], or pairs[kTile]) | cnt16 | toff | gofs | last
+  // Layout: stage (keys[kTile] + vals[kTile], or pairs[kTile]) | cnt16 | toff | gofs
+  int32_t *s_keys = reinterpret_cast<int32_t *>(smem);
+  int32_t *s_vals = s_keys + kTile;  // SOA only
+  int2 *s_pairs = reinterpret_cast<int2 *>(smem);  // AOS only
   const size_t stage = kKV ? kTile * 8 : kTile * 4;
-  uint16_t *cnt16 = reinterpret_cast<uint16_t *>(smem + NBUF * stage);
+  uint16_t *cnt16 = reinterpret_cast<uint16_t *>(smem + stage);
   int32_t *toff = reinterpret_cast<int32_t *>(
-      smem + NBUF * stage + round_up(static_cast<size_t>(C::kWarps) * buckets * 2, 16));
+      smem + stage + round_up(static_cast<size_t>(C::kWarps) * buckets * 2, 16));
   int32_t *gofs = toff + buckets;
   uint8_t *s_last = reinterpret_cast<uint8_t *>(gofs + buckets);  // [kWarps][min(buckets, 256)]
-  __shared__ alignas(8) uint64_t bar[2];
+  __shared__ alignas(8) uint64_t bar;
 
+  const int64_t t = blockIdx.x;
+  const int64_t base = t * kTile;
+  const int count = static_cast<int>(min64(kTile, n - base));
   const unsigned mask = static_cast<unsigned>(buckets - 1);
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-  const int64_t G = gridDim.x;
-  auto count_of = [&](int64_t tl) { return static_cast<int>(min64(kTile, n - tl * kTile)); };
-  auto bulk_of = [&](int64_t tl) -> uint32_t {
-    if (!tma) return 0u;
-    const int c = count_of(tl);
-    return static_cast<uint32_t>((LAYOUT == EDPP_KVS_AOS) ? (c & ~1) : (c & ~3));
-  };
-  // thread 0: bulk copies of tile tl's 16-byte-aligned prefix into buffer k
-  auto issue = [&](int64_t tl, int k) {
-    const uint32_t be = bulk_of(tl);
-    if (!be) return;
-    unsigned char *buf = smem + k * stage;
-    const int64_t base = tl * kTile;
-    if (LAYOUT == EDPP_KVS_AOS) {
-      mbar_arrive_expect_tx(&bar[k], be * 8);
-      tma_load_1d(buf, keys_in + 2 * base, be * 8, &bar[k]);
-    } else if (LAYOUT == EDPP_KVS_SOA) {
-      mbar_arrive_expect_tx(&bar[k], be * 8);
-      tma_load_1d(buf, keys_in + base, be * 4, &bar[k]);
-      tma_load_1d(buf + kTile * 4, vals_in + base, be * 4, &bar[k]);
-    } else {
-      mbar_arrive_expect_tx(&bar[k], be * 4);
-      tma_load_1d(buf, keys_in + base, be * 4, &bar[k]);
-    }
-  };
+
+  // -- load the tile (bulk copies for the 16-byte-aligned prefix) --
   if (tid == 0) {
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
+    mbar_init(&bar, 1);
     fence_mbar_init();
-    for (int k = 0; k < NBUF; ++k)
-      if (blockIdx.x + k * G < tiles) issue(blockIdx.x + k * G, k);
   }
   __syncthreads();
-  uint32_t phase = 0;  // bit k: parity of bar[k]'s next completion
-  int bk = 0;
-  for (int64_t t = blockIdx.x; t < tiles; t += G, bk = (NBUF == 2 ? bk ^ 1 : 0)) {
-  int32_t *s_keys = reinterpret_cast<int32_t *>(smem + bk * stage);
-  int32_t *s_vals = s_keys + kTile;  // SOA only
-  int2 *s_pairs = reinterpret_cast<int2 *>(smem + bk * stage);  // AOS only
-  const int64_t base = t * kTile;
-  const int count = count_of(t);
-  const uint32_t bulk_elems = bulk_of(t);
-  // -- the tile: bulk-copied prefix (waited on below) plus plain loads --
+  uint32_t bulk_elems = 0;
+  if (tma) bulk_elems = (LAYOUT == EDPP_KVS_AOS) ? (count & ~1) : (count & ~3);
+  if (tid == 0 && bulk_elems) {
+    if (LAYOUT == EDPP_KVS_AOS) {
+      mbar_arrive_expect_tx(&bar, bulk_elems * 8);
+      tma_load_1d(s_pairs, keys_in + 2 * base, bulk_elems * 8, &bar);
+    } else if (LAYOUT == EDPP_KVS_SOA) {
+      mbar_arrive_expect_tx(&bar, bulk_elems * 8);
+      tma_load_1d(s_keys, keys_in + base, bulk_elems * 4, &bar);
+      tma_load_1d(s_vals, vals_in + base, bulk_elems * 4, &bar);
+    } else {
+      mbar_arrive_expect_tx(&bar, bulk_elems * 4);
+      tma_load_1d(s_keys, keys_in + base, bulk_elems * 4, &bar);
+    }
+  }
   for (int i = static_cast<int>(bulk_elems) + tid; i < count; i += THREADS) {
     if (LAYOUT == EDPP_KVS_AOS) {
       s_pairs[i] = make_int2(keys_in[2 * (base + i)], keys_in[2 * (base + i) + 1]);
@@ -192,12 +173,10 @@ __global__ void __launch_bounds__(THREADS, 2)
     }
   }
   for (int i = tid; i < C::kWarps * buckets; i += THREADS) cnt16[i] = 0;
-  bool bad = false;
   if (bulk_elems) {
-    bad = !mbar_wait_bounded(&bar[bk], (phase >> bk) & 1u, timeout_ns, fault);
-    phase ^= 1u << bk;
+    if (!mbar_wait_bounded(&bar, 0, timeout_ns, fault)) return;
   }
-  if (__syncthreads_or(bad)) return;
+  __syncthreads();
 
   // -- rank: warp w owns tile positions [w*kSeg, (w+1)*kSeg), in order --
   const unsigned lt = lanemask_lt();
@@ -349,13 +328,6 @@ __global__ void __launch_bounds__(THREADS, 2)
       if (LAYOUT == EDPP_KVS_SOA) vals_out[o] = s_vals[s];
     }
   }
-  if (NBUF == 1) break;
-  // generic accesses of this buffer, gofs and the counters end before the
-  // next tile's bulk copy into it and the next tile's counting
-  fence_proxy_async_smem();
-  __syncthreads();
-  if (tid == 0 && t + 2 * G < tiles) issue(t + 2 * G, bk);
-  }
 }
 
 // bucket_start[b] = his[b*T] (gatherStartPos, split_kernel.cl:320-332).
@@ -369,7 +341,7 @@ size_t his_bytes(int64_t tiles, int buckets) {
   return round_up(static_cast<size_t>(tiles) * buckets * 4, 256);
 }
 
-template <int THREADS, int LAYOUT, int NBUF> int set_smem_attr() {
+template <int THREADS, int LAYOUT> int set_smem_attr() {
   static std::once_flag once[64];
   static int status[64];
   int dev = 0;
@@ -377,32 +349,22 @@ template <int THREADS, int LAYOUT, int NBUF> int set_smem_attr() {
   if (dev < 0 || dev >= 64) dev = 0;
   std::call_once(once[dev], [&] {
     // 512 threads serve up to 1024 buckets, 256 threads the rest
-    const size_t bytes =
-        scatter_smem_bytes<THREADS, LAYOUT, NBUF>(THREADS == 512 ? 1024 : kMaxBuckets);
-    status[dev] = cuda_status(cudaFuncSetAttribute(split_scatter_kernel<THREADS, LAYOUT, NBUF>,
+    const size_t bytes = scatter_smem_bytes<THREADS, LAYOUT>(THREADS == 512 ? 1024 : kMaxBuckets);
+    status[dev] = cuda_status(cudaFuncSetAttribute(split_scatter_kernel<THREADS, LAYOUT>,
                                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                    static_cast<int>(bytes)));
   });
   return status[dev];
 }
 
-// NBUF == 2 runs persistent blocks, as many as stay resident.
-template <int THREADS, int LAYOUT, int NBUF>
+template <int THREADS, int LAYOUT>
 int launch_scatter(const int32_t *keys_in, int32_t *keys_out, const int32_t *vals_in,
                    int32_t *vals_out, int64_t n, int buckets, int shift, int64_t tiles,
                    const int32_t *his, bool tma, cudaStream_t st) {
-  const int s = set_smem_attr<THREADS, LAYOUT, NBUF>();
+  const int s = set_smem_attr<THREADS, LAYOUT>();
   if (s != EDPP_OK) return s;
-  const size_t smem = scatter_smem_bytes<THREADS, LAYOUT, NBUF>(buckets);
-  int64_t grid = tiles;
-  if (NBUF == 2) {
-    int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &per_sm, split_scatter_kernel<THREADS, LAYOUT, NBUF>, THREADS, smem) != cudaSuccess)
-      return EDPP_ECUDA;
-    grid = min64(tiles, static_cast<int64_t>(device_sm_count()) * max64(per_sm, 1));
-  }
-  split_scatter_kernel<THREADS, LAYOUT, NBUF><<<static_cast<unsigned>(grid), THREADS, smem, st>>>(
+  const size_t smem = scatter_smem_bytes<THREADS, LAYOUT>(buckets);
+  split_scatter_kernel<THREADS, LAYOUT><<<static_cast<unsigned>(tiles), THREADS, smem, st>>>(
       keys_in, keys_out, vals_in, vals_out, n, buckets, shift, tiles, his, tma, kDefaultWaitNs,
       fault_word());
   return launch_status();
@@ -430,10 +392,10 @@ int split_layout(const int32_t *keys_in, int32_t *keys_out, int32_t *bucket_star
     if (s != EDPP_OK) return s;
   }
   if (buckets <= 1024)
-    return launch_scatter<512, LAYOUT, 2>(keys_in, keys_out, vals_in, vals_out, n, buckets, shift,
-                                          tiles, his, tma, st);
-  return launch_scatter<256, LAYOUT, 1>(keys_in, keys_out, vals_in, vals_out, n, buckets, shift,
-                                        tiles, his, tma, st);
+    return launch_scatter<512, LAYOUT>(keys_in, keys_out, vals_in, vals_out, n, buckets, shift,
+                                       tiles, his, tma, st);
+  return launch_scatter<256, LAYOUT>(keys_in, keys_out, vals_in, vals_out, n, buckets, shift,
+                                     tiles, his, tma, st);
 }
 
 size_t split_ws_bytes(int64_t n, int buckets) {
