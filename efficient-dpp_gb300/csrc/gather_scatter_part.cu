@@ -246,11 +246,8 @@ __global__ void __launch_bounds__(kThreads)
 // into shared memory by TMA (loc, and in for a scatter, on one barrier) while
 // the current one is grouped; the landed buffer then serves as the staging
 // area of the runs.  Same output as part_partition_kernel.
-constexpr int kPThreads = 512;                // pipelined partition block
-constexpr int kPPer = kTile / kPThreads;       // 8 elements per thread per tile
-
 template <bool kScatter>
-__global__ void __launch_bounds__(kPThreads, 2)
+__global__ void __launch_bounds__(kThreads, 2)
     part_partition_pipe_kernel(const int32_t *__restrict__ loc, const int32_t *__restrict__ in,
                                int64_t n, int log_w, int nwin, uint32_t *__restrict__ fill,
                                int2 *__restrict__ pairs, uint64_t timeout_ns, unsigned *fault) {
@@ -260,7 +257,7 @@ __global__ void __launch_bounds__(kPThreads, 2)
   uint32_t *soff = scnt + nwin;
   uint32_t *sgb = soff + nwin;
   __shared__ alignas(8) uint64_t bar[2];
-  __shared__ uint32_t s_warp[kPThreads / 32 + 1];
+  __shared__ uint32_t s_warp[16];
   const int t = threadIdx.x;
   const int64_t G = gridDim.x;
   const int64_t tiles = (n + kTile - 1) / kTile;
@@ -298,20 +295,20 @@ __global__ void __launch_bounds__(kPThreads, 2)
       bad = !mbar_wait_bounded(&bar[b], (phase >> b) & 1u, timeout_ns, fault);
       phase ^= 1u << b;
     }
-    for (int i = static_cast<int>(bytes / 4) + t; i < count; i += kPThreads) {
+    for (int i = static_cast<int>(bytes / 4) + t; i < count; i += kThreads) {
       buf[i] = loc[base + i];
       if (kScatter) buf[kTile + i] = in[base + i];
     }
-    for (int i = t; i < nwin; i += kPThreads) scnt[i] = 0;
+    for (int i = t; i < nwin; i += kThreads) scnt[i] = 0;
     if (__syncthreads_or(bad)) {
       failed = true;
       break;
     }
-    int2 pr[kPPer];
-    int w[kPPer], rank[kPPer];
+    int2 pr[kPer];
+    int w[kPer], rank[kPer];
 #pragma unroll
-    for (int k = 0; k < kPPer / 4; ++k) {
-      const int i0 = (k * kPThreads + t) * 4;
+    for (int k = 0; k < kPer / 4; ++k) {
+      const int i0 = (k * kThreads + t) * 4;
       const int4 l = *reinterpret_cast<const int4 *>(buf + i0);
       int4 v = make_int4(0, 0, 0, 0);
       if (kScatter) v = *reinterpret_cast<const int4 *>(buf + kTile + i0);
@@ -327,7 +324,7 @@ __global__ void __launch_bounds__(kPThreads, 2)
       }
     }
     __syncthreads();  // counts complete; every read of buf done
-    flush_runs<kPPer, kPThreads>(pr, w, rank, nwin, log_w, scnt, soff, sgb, s_warp,
+    flush_runs<kPer>(pr, w, rank, nwin, log_w, scnt, soff, sgb, s_warp,
                      reinterpret_cast<int2 *>(buf), fill, pairs);
     fence_proxy_async_smem();  // generic accesses of buf before the next bulk copy into it
     __syncthreads();
@@ -548,10 +545,10 @@ int launch_partition(const int32_t *loc, const int32_t *in, int64_t n, int log_w
   const size_t smem = part_pipe_smem(nwin);
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, part_partition_pipe_kernel<kScatter>,
-                                                    kPThreads, smem) != cudaSuccess)
+                                                    kThreads, smem) != cudaSuccess)
     return EDPP_ECUDA;
   const int64_t blocks = min64(tiles, static_cast<int64_t>(device_sm_count()) * max64(per_sm, 1));
-  part_partition_pipe_kernel<kScatter><<<static_cast<unsigned>(blocks), kPThreads, smem, st>>>(
+  part_partition_pipe_kernel<kScatter><<<static_cast<unsigned>(blocks), kThreads, smem, st>>>(
       loc, in, n, log_w, nwin, fill, pairs, kDefaultWaitNs, fault);
   return launch_status();
 }
@@ -738,9 +735,7 @@ __global__ void __launch_bounds__(1024)
 // memory (the landed input buffer is reused as the staging area) and written
 // as one run per window; a wider one (skewed keys) appends pair by pair.
 constexpr int kRefineSpan = 512;
-constexpr int kRefineBlocksPerSm = 2;
-constexpr int kRThreads = 512;                  // refine block
-constexpr int kRPer = kTile / kRThreads;        // 8 pairs per thread per tile
+constexpr int kRefineBlocksPerSm = 3;
 
 __device__ __forceinline__ void refine_range(int64_t slot, const uint32_t *total_p,
                                              const uint32_t *region_end, int region_log,
@@ -766,7 +761,7 @@ __device__ __forceinline__ void refine_issue(const int2 *src, int64_t lo, int64_
   }
 }
 
-__global__ void __launch_bounds__(kRThreads, kRefineBlocksPerSm)
+__global__ void __launch_bounds__(kThreads, kRefineBlocksPerSm)
     win_refine_kernel(const int2 *__restrict__ src, const uint32_t *__restrict__ total_p,
                       const uint32_t *__restrict__ region_end, int region_log, int fine_log,
                       int64_t slots, uint32_t *__restrict__ fill, int2 *__restrict__ dst,
@@ -777,7 +772,7 @@ __global__ void __launch_bounds__(kRThreads, kRefineBlocksPerSm)
   uint32_t *soff = scnt + kRefineSpan;
   uint32_t *sgb = soff + kRefineSpan;
   __shared__ alignas(8) uint64_t bar[2];
-  __shared__ uint32_t s_warp[kRThreads / 32 + 1];
+  __shared__ uint32_t s_warp[16];
   __shared__ int s_lo, s_hi;
   const int t = threadIdx.x;
   const int64_t G = gridDim.x;
@@ -816,17 +811,17 @@ __global__ void __launch_bounds__(kRThreads, kRefineBlocksPerSm)
         s_lo = INT_MAX;
         s_hi = -1;
       }
-      for (int i = t; i < kRefineSpan; i += kRThreads) scnt[i] = 0;
+      for (int i = t; i < kRefineSpan; i += kThreads) scnt[i] = 0;
       if (__syncthreads_or(bad)) {
         failed = true;
         break;
       }
-      int2 pr[kRPer];
-      int fid[kRPer];
+      int2 pr[kPer];
+      int fid[kPer];
       int my_lo = INT_MAX, my_hi = -1;
 #pragma unroll
-      for (int k = 0; k < kRPer / 2; ++k) {
-        const uint32_t j = static_cast<uint32_t>(k * kRThreads + t) * 2u;
+      for (int k = 0; k < kPer / 2; ++k) {
+        const uint32_t j = static_cast<uint32_t>(k * kThreads + t) * 2u;
         int4 q = make_int4(0, 0, 0, 0);
         if (j + 1 < cnt) q = *reinterpret_cast<const int4 *>(buf + j);
         else if (j < cnt) { const int2 a = buf[j]; q.x = a.x; q.y = a.y; }
@@ -836,7 +831,7 @@ __global__ void __launch_bounds__(kRThreads, kRefineBlocksPerSm)
         fid[2 * k + 1] = j + 1 < cnt ? (q.z >> fine_log) : -1;
       }
 #pragma unroll
-      for (int e = 0; e < kRPer; ++e)
+      for (int e = 0; e < kPer; ++e)
         if (fid[e] >= 0) {
           my_lo = min(my_lo, fid[e]);
           my_hi = max(my_hi, fid[e]);
@@ -854,29 +849,29 @@ __global__ void __launch_bounds__(kRThreads, kRefineBlocksPerSm)
       const int wlo = s_lo, span = s_hi - s_lo + 1;
       if (span > kRefineSpan) {  // skewed slot: one cursor claim per pair
 #pragma unroll
-        for (int e = 0; e < kRPer; ++e)
+        for (int e = 0; e < kPer; ++e)
           if (fid[e] >= 0) dst[atomicAdd(&fill[fid[e]], 1u)] = pr[e];
       } else {
-        int rank[kRPer];
+        int rank[kPer];
 #pragma unroll
-        for (int e = 0; e < kRPer; ++e) {
+        for (int e = 0; e < kPer; ++e) {
           fid[e] = fid[e] >= 0 ? fid[e] - wlo : -1;
           rank[e] = rank_in_window(fid[e], scnt, lt);
         }
         __syncthreads();
-        const uint32_t total = block_scan_counts<kRThreads>(scnt, soff, span, s_warp);
+        const uint32_t total = block_scan_counts(scnt, soff, span, s_warp);
         // run start minus staging offset; the first claim's round trip
         // overlaps the staging writes
         const uint32_t c0 = t < span ? scnt[t] : 0u;
         const uint32_t g0 = c0 ? atomicAdd(&fill[wlo + t], c0) : 0u;
-        for (int i = t + kRThreads; i < span; i += kRThreads)
+        for (int i = t + kThreads; i < span; i += kThreads)
           if (scnt[i]) sgb[i] = atomicAdd(&fill[wlo + i], scnt[i]) - soff[i];
 #pragma unroll
-        for (int e = 0; e < kRPer; ++e)
+        for (int e = 0; e < kPer; ++e)
           if (fid[e] >= 0) buf[soff[fid[e]] + rank[e]] = pr[e];
         if (c0) sgb[t] = g0 - soff[t];
         __syncthreads();
-        for (uint32_t q = t; q < total; q += kRThreads) {
+        for (uint32_t q = t; q < total; q += kThreads) {
           const int2 p = buf[q];
           dst[sgb[(p.x >> fine_log) - wlo] + q] = p;
         }
@@ -1118,7 +1113,7 @@ int tiled_run(const int32_t *in, int32_t *out, int64_t n, const int32_t *loc, in
   unsigned *fault = fault_word();
   if (!fault) return EDPP_ECUDA;
   const int64_t rblocks = static_cast<int64_t>(sms) * kRefineBlocksPerSm;
-  win_refine_kernel<<<static_cast<unsigned>(min64(tiles, rblocks)), kRThreads, refine_smem(), st>>>(
+  win_refine_kernel<<<static_cast<unsigned>(min64(tiles, rblocks)), kThreads, refine_smem(), st>>>(
       pa, start + p.F, nullptr, 0, p.fine_log, tiles, fill, pb, kDefaultWaitNs, fault);
   if (kScatter) {
     win_apply_kernel<<<static_cast<unsigned>(p.F), kWinThreads, apply_smem(p.fine_log), st>>>(
@@ -1127,7 +1122,7 @@ int tiled_run(const int32_t *in, int32_t *out, int64_t n, const int32_t *loc, in
     win_fetch_kernel<<<static_cast<unsigned>(p.F), kFetchThreads, fetch_smem(p.fine_log, p.C), st>>>(
         pb, start, in, n, p.fine_log, p.coarse_log, p.C, cfill2, pa, vec_in, kDefaultWaitNs, fault);
     const int64_t rtiles = static_cast<int64_t>(p.C) << (p.coarse_log - 12);
-    win_refine_kernel<<<static_cast<unsigned>(min64(rtiles, rblocks)), kRThreads, refine_smem(), st>>>(
+    win_refine_kernel<<<static_cast<unsigned>(min64(rtiles, rblocks)), kThreads, refine_smem(), st>>>(
         pa, nullptr, cfill2, p.coarse_log, p.fine_log, rtiles, fill2, pb, kDefaultWaitNs, fault);
     win_apply_kernel<<<static_cast<unsigned>(p.F), kWinThreads, apply_smem(p.fine_log), st>>>(
         pb, nullptr, fill2, p.fine_log, n, out, aligned16(out));
