@@ -106,7 +106,7 @@ __device__ void block_exclusive_scan_inplace(int32_t *p, int64_t m, int32_t *wsu
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 3)
     batch_kernel(const DevSeg *__restrict__ segs, const DevTask *__restrict__ tasks, int num_tasks,
                  const int32_t *__restrict__ in0, const int32_t *__restrict__ in1,
                  int32_t *__restrict__ out0, int32_t *__restrict__ out1, char *state,
