@@ -146,3 +146,17 @@ def test_against_reference_cuda_kernels(cuda, edpp, orc):
             for method in METHODS:
                 mine = to_host(f(to_dev(inp), to_dev(loc), passes, method=method))
                 np.testing.assert_array_equal(mine, ref)
+
+
+def test_tiled_above_2p29_takes_the_l2_window_path(cuda, edpp):
+    # beyond 2^29 elements the tiled entry points hand over to the L2-window
+    # partition (pass 0) inside the same workspace; identity properties
+    n = (1 << 29) + 7
+    loc = to_dev(edpp.gen_permutation(n, 2))
+    inp = cuda.arange(n, dtype=cuda.int32, device="cuda")
+    ws = edpp.workspace(edpp.gs_workspace_bytes("gather", n, 1, "tiled"))
+    g = edpp.gather(inp, loc, 1, method="tiled", ws=ws)
+    assert cuda.equal(g, loc)
+    del g
+    s = edpp.scatter(inp, loc, 1, method="tiled", ws=ws)
+    assert cuda.equal(edpp.gather(s, loc, 1, method="tiled", ws=ws), inp)
