@@ -917,6 +917,10 @@ def main(argv=None):
         gbs = call_bytes(name, n) / (ms * 1e-3) / 1e9
         primitives[key] = {"ms": round(ms, 4), "GB/s": round(gbs, 1),
                            "frac_of_hbm": round(gbs / peak, 4)}
+        if name in ("gather", "scatter"):
+            # the reference's own figure: n * 4 bytes / time in GiB/s
+            # (cuda/util/utility.cuh:15-17, opencl/test/test_gather.cpp:50)
+            primitives[key]["reference_formula_GiB/s"] = round(n * 4 / (ms * 1e-3) / 2**30, 1)
     dom = max(per_call_ms, key=lambda c: per_call_ms[c])
     dom_name = f"{dom[0]}_p{dom[1]}" if dom[1] else dom[0]
     # The dominant call of the step: its algorithmic bytes over its CUDA-event
