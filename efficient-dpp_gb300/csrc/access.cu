@@ -49,23 +49,34 @@ __global__ void scale_mixed_kernel(const int32_t *__restrict__ in, int32_t *__re
   for (int i = 0; i < repeat; ++i, idx += 32) out[idx] = in[idx] * kScalar;
 }
 
-// vector: 16-byte grid-stride loop over the same n elements, scalar tail
+// vector: 16-byte grid-stride loop over the same n elements, four vectors
+// in flight per thread before the stores (the STREAM kernels' shape),
+// scalar tail
 __global__ void scale_vec_kernel(const int32_t *__restrict__ in, int32_t *__restrict__ out,
                                  int64_t n) {
+  constexpr int kU = 4;
   const int64_t G = static_cast<int64_t>(gridDim.x) * blockDim.x;
-  const int64_t g = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   const int64_t nv = n >> 2;
   const int4 *vi = reinterpret_cast<const int4 *>(in);
   int4 *vo = reinterpret_cast<int4 *>(out);
-  for (int64_t i = g; i < nv; i += G) {
-    int4 v = __ldcs(vi + i);
+  auto scale4 = [](int4 v) {
     v.x *= kScalar;
     v.y *= kScalar;
     v.z *= kScalar;
     v.w *= kScalar;
-    __stcs(vo + i, v);
+    return v;
+  };
+  for (; i + (kU - 1) * G < nv; i += kU * G) {
+    int4 v[kU];
+#pragma unroll
+    for (int u = 0; u < kU; ++u) v[u] = __ldcs(vi + i + u * G);
+#pragma unroll
+    for (int u = 0; u < kU; ++u) __stcs(vo + i + u * G, scale4(v[u]));
   }
-  for (int64_t i = (nv << 2) + g; i < n; i += G) out[i] = in[i] * kScalar;
+  for (; i < nv; i += G) __stcs(vo + i, scale4(__ldcs(vi + i)));
+  const int64_t g = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  for (int64_t j = (nv << 2) + g; j < n; j += G) out[j] = in[j] * kScalar;
 }
 
 // Block b takes ticket t (atomic), visits chunk order[t] of `len / blocks`
