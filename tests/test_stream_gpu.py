@@ -47,3 +47,21 @@ def test_against_reference_cuda_kernels(cuda, edpp, orc, op):
     assert rc.refcu_stream_i32(op, P(a), P(b), P(ref), n) == 0
     name = ["copy", "scale", "add", "triad"][op]
     np.testing.assert_array_equal(to_host(edpp.stream(name, to_dev(a), to_dev(b), 3)), ref)
+
+
+@pytest.mark.parametrize("op", ["copy", "scale", "add", "triad"])
+def test_large_arrays_one_vector_per_thread(cuda, edpp, op):
+    # 2^26 elements and more take the one-vector-per-thread kernel; a ragged
+    # tail of 3 elements; f32 results equal the same IEEE operations in torch
+    torch = cuda
+    n = (1 << 26) + 3
+    a = torch.arange(n, dtype=torch.float32, device="cuda")
+    b = a + 10
+    c = edpp.stream(op, a, b, 3.0)
+    want = {"copy": a, "scale": a * 3.0, "add": a + b, "triad": a + b * 3.0}[op]
+    assert torch.equal(c, want)
+    ai = torch.arange(n, dtype=torch.int32, device="cuda") * 7919
+    bi = ai + 10
+    ci = edpp.stream(op, ai, bi, 3)
+    wi = {"copy": ai, "scale": ai * 3, "add": ai + bi, "triad": ai + bi * 3}[op]
+    assert torch.equal(ci, wi)
