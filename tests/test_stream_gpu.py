@@ -52,13 +52,16 @@ def test_against_reference_cuda_kernels(cuda, edpp, orc, op):
 @pytest.mark.parametrize("op", ["copy", "scale", "add", "triad"])
 def test_large_arrays_one_vector_per_thread(cuda, edpp, op):
     # 2^26 elements and more take the one-vector-per-thread kernel; a ragged
-    # tail of 3 elements; f32 results equal the same IEEE operations in torch
+    # tail of 3 elements.  f32 copy/scale/add are single IEEE operations;
+    # triad a + 3b is one fused multiply-add (as nvcc compiles the
+    # reference's kernels), i.e. the exact value rounded once
     torch = cuda
     n = (1 << 26) + 3
     a = torch.arange(n, dtype=torch.float32, device="cuda")
     b = a + 10
     c = edpp.stream(op, a, b, 3.0)
-    want = {"copy": a, "scale": a * 3.0, "add": a + b, "triad": a + b * 3.0}[op]
+    fused = (a.double() + b.double() * 3.0).float()
+    want = {"copy": a, "scale": a * 3.0, "add": a + b, "triad": fused}[op]
     assert torch.equal(c, want)
     ai = torch.arange(n, dtype=torch.int32, device="cuda") * 7919
     bi = ai + 10
