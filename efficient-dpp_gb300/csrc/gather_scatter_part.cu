@@ -193,6 +193,64 @@ __device__ __forceinline__ void flush_runs(const int2 (&pr)[PER], const int (&w)
   }
 }
 
+// The pipelined stages (partition, refine, fetch) group a tile with four
+// barriers: (A) rank atomics done; claim_runs; (B) staging offsets known;
+// staging writes and publish_run_bases; (C) runs staged; read-out.
+//
+// claim_runs, between A and B: thread t owns windows [t*per, t*per + per),
+// per = ceil(nwin / NT) <= MAXPER.  For each owned window with pairs it
+// claims the tile's run at the window's global cursor (g), resets the
+// counter for the next tile, and sets the window's staging offset (o, and
+// soff[] for the staging writes).  Warps take their part of the staging area
+// in arrival order, by one shared atomic on *s_total (zero on entry; the
+// tile's pair count after B): windows need disjoint contiguous ranges, not
+// ordered ones.  The claims are consumed only by publish_run_bases, after
+// the staging writes, so their round trip to L2 overlaps both.
+template <int MAXPER, int NT>
+__device__ __forceinline__ void claim_runs(uint32_t *scnt, uint32_t *soff, int nwin,
+                                           uint32_t *__restrict__ fill, uint32_t *s_total,
+                                           uint32_t (&g)[MAXPER], uint32_t (&o)[MAXPER]) {
+  const int lane = threadIdx.x & 31;
+  const int per = (nwin + NT - 1) / NT;
+  const int lo = static_cast<int>(threadIdx.x) * per;
+  uint32_t s = 0;
+#pragma unroll
+  for (int k = 0; k < MAXPER; ++k) {
+    const int i = lo + k;
+    const uint32_t c = (k < per && i < nwin) ? scnt[i] : 0u;
+    g[k] = c ? atomicAdd(&fill[i], c) : 0u;
+    if (c) scnt[i] = 0u;
+    o[k] = s;
+    s += c;
+  }
+  uint32_t incl = s;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d) incl += y;
+  }
+  uint32_t wb = 0;
+  if (lane == 31 && incl) wb = atomicAdd(s_total, incl);
+  const uint32_t base = __shfl_sync(0xffffffffu, wb, 31) + incl - s;
+#pragma unroll
+  for (int k = 0; k < MAXPER; ++k) {
+    o[k] += base;
+    if (k < per && lo + k < nwin) soff[lo + k] = o[k];
+  }
+}
+
+// sgb[w] = global index of window w's run minus its staging offset (modulo
+// 2^32), so a staged slot s maps to dst[sgb[w] + s].
+template <int MAXPER, int NT>
+__device__ __forceinline__ void publish_run_bases(uint32_t *sgb, int nwin, const uint32_t (&g)[MAXPER],
+                                                  const uint32_t (&o)[MAXPER]) {
+  const int per = (nwin + NT - 1) / NT;
+  const int lo = static_cast<int>(threadIdx.x) * per;
+#pragma unroll
+  for (int k = 0; k < MAXPER; ++k)
+    if (k < per && lo + k < nwin) sgb[lo + k] = g[k] - o[k];
+}
+
 // ---- partition -------------------------------------------------------------------
 // Gather pairs {loc, i}; scatter pairs {loc, in[i]}.
 template <bool kScatter>
@@ -245,8 +303,10 @@ __global__ void __launch_bounds__(kThreads)
 // blocks take tiles blockIdx, +gridDim, ...; the tile after next is copied
 // into shared memory by TMA (loc, and in for a scatter, on one barrier) while
 // the current one is grouped; the landed buffer then serves as the staging
-// area of the runs.  Same output as part_partition_kernel.
-template <bool kScatter>
+// area of the runs.  Elements past the bulk copy (a ragged last tile) are read
+// from global memory by the thread that ranks them.  nwin <= MAXPER * kThreads.
+// Same output as part_partition_kernel.
+template <bool kScatter, int MAXPER>
 __global__ void __launch_bounds__(kThreads, 2)
     part_partition_pipe_kernel(const int32_t *__restrict__ loc, const int32_t *__restrict__ in,
                                int64_t n, int log_w, int nwin, uint32_t *__restrict__ fill,
@@ -257,7 +317,7 @@ __global__ void __launch_bounds__(kThreads, 2)
   uint32_t *soff = scnt + nwin;
   uint32_t *sgb = soff + nwin;
   __shared__ alignas(8) uint64_t bar[2];
-  __shared__ uint32_t s_warp[16];
+  __shared__ uint32_t s_total;
   const int t = threadIdx.x;
   const int64_t G = gridDim.x;
   const int64_t tiles = (n + kTile - 1) / kTile;
@@ -272,7 +332,9 @@ __global__ void __launch_bounds__(kThreads, 2)
     tma_load_1d(buf, loc + tl * kTile, bytes, b);
     if (kScatter) tma_load_1d(buf + kTile, in + tl * kTile, bytes, b);
   };
+  for (int i = t; i < nwin; i += kThreads) scnt[i] = 0;
   if (t == 0) {
+    s_total = 0;
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
     fence_mbar_init();
@@ -280,7 +342,6 @@ __global__ void __launch_bounds__(kThreads, 2)
       if (blockIdx.x + k * G < tiles) issue(blockIdx.x + k * G, bufs + k * 2 * kTile, &bar[k]);
   }
   __syncthreads();
-  const unsigned lt = lanemask_lt();
   uint32_t phase = 0;
   int b = 0;
   int64_t tl = blockIdx.x;
@@ -290,42 +351,63 @@ __global__ void __launch_bounds__(kThreads, 2)
     const int64_t base = tl * kTile;
     const int count = static_cast<int>(min64(kTile, n - base));
     const uint32_t bytes = bulk_of(tl);
+    const int nb = static_cast<int>(bytes / 4);  // a multiple of 4
     bool bad = false;
     if (bytes) {
       bad = !mbar_wait_bounded(&bar[b], (phase >> b) & 1u, timeout_ns, fault);
       phase ^= 1u << b;
-    }
-    for (int i = static_cast<int>(bytes / 4) + t; i < count; i += kThreads) {
-      buf[i] = loc[base + i];
-      if (kScatter) buf[kTile + i] = in[base + i];
-    }
-    for (int i = t; i < nwin; i += kThreads) scnt[i] = 0;
-    if (__syncthreads_or(bad)) {
-      failed = true;
-      break;
     }
     int2 pr[kPer];
     int w[kPer], rank[kPer];
 #pragma unroll
     for (int k = 0; k < kPer / 4; ++k) {
       const int i0 = (k * kThreads + t) * 4;
-      const int4 l = *reinterpret_cast<const int4 *>(buf + i0);
-      int4 v = make_int4(0, 0, 0, 0);
-      if (kScatter) v = *reinterpret_cast<const int4 *>(buf + kTile + i0);
-      const int32_t ls[4] = {l.x, l.y, l.z, l.w};
-      const int32_t vs[4] = {v.x, v.y, v.z, v.w};
+      int32_t ls[4] = {-1, -1, -1, -1}, vs[4] = {0, 0, 0, 0};
+      if (i0 < nb) {
+        if (!bad) {
+          const int4 l = *reinterpret_cast<const int4 *>(buf + i0);
+          ls[0] = l.x, ls[1] = l.y, ls[2] = l.z, ls[3] = l.w;
+          if (kScatter) {
+            const int4 v = *reinterpret_cast<const int4 *>(buf + kTile + i0);
+            vs[0] = v.x, vs[1] = v.y, vs[2] = v.z, vs[3] = v.w;
+          }
+        }
+      } else {
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if (i0 + q < count) {
+            ls[q] = loc[base + i0 + q];
+            if (kScatter) vs[q] = in[base + i0 + q];
+          }
+      }
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         const int e = 4 * k + q;
         const bool valid = (i0 + q < count) && ls[q] >= 0 && static_cast<int64_t>(ls[q]) < n;
         w[e] = valid ? (ls[q] >> log_w) : -1;
         pr[e] = make_int2(ls[q], kScatter ? vs[q] : static_cast<int32_t>(base + i0 + q));
-        rank[e] = rank_in_window(w[e], scnt, lt);
+        rank[e] = valid ? static_cast<int>(atomicAdd(&scnt[w[e]], 1u)) : -1;
       }
     }
-    __syncthreads();  // counts complete; every read of buf done
-    flush_runs<kPer>(pr, w, rank, nwin, log_w, scnt, soff, sgb, s_warp,
-                     reinterpret_cast<int2 *>(buf), fill, pairs);
+    if (__syncthreads_or(bad)) {  // A: counts complete; every read of buf done
+      failed = true;
+      break;
+    }
+    uint32_t g[MAXPER], o[MAXPER];
+    claim_runs<MAXPER, kThreads>(scnt, soff, nwin, fill, &s_total, g, o);
+    __syncthreads();  // B
+    const uint32_t total = s_total;
+    int2 *stage = reinterpret_cast<int2 *>(buf);
+#pragma unroll
+    for (int e = 0; e < kPer; ++e)
+      if (w[e] >= 0) stage[soff[w[e]] + rank[e]] = pr[e];
+    publish_run_bases<MAXPER, kThreads>(sgb, nwin, g, o);
+    __syncthreads();  // C
+    if (t == 0) s_total = 0;
+    for (uint32_t s = t; s < total; s += kThreads) {
+      const int2 p = stage[s];
+      pairs[sgb[p.x >> log_w] + s] = p;
+    }
     fence_proxy_async_smem();  // generic accesses of buf before the next bulk copy into it
     __syncthreads();
     if (t == 0 && tl + 2 * G < tiles) issue(tl + 2 * G, buf, &bar[b]);
@@ -516,14 +598,17 @@ int ensure_attrs() {
     if (d < 0 || d >= 64) d = 0;
     int s = set_smem(part_partition_kernel<false>);
     if (s == EDPP_OK) s = set_smem(part_partition_kernel<true>);
+    const int pipe_smem = static_cast<int>(part_pipe_smem(kMaxWin));
+    auto pipe = [&](const void *k) {
+      return cuda_status(
+          cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, pipe_smem));
+    };
+    if (s == EDPP_OK) s = pipe(reinterpret_cast<const void *>(part_partition_pipe_kernel<false, 1>));
+    if (s == EDPP_OK) s = pipe(reinterpret_cast<const void *>(part_partition_pipe_kernel<true, 1>));
     if (s == EDPP_OK)
-      s = cuda_status(cudaFuncSetAttribute(part_partition_pipe_kernel<false>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           static_cast<int>(part_pipe_smem(kMaxWin))));
+      s = pipe(reinterpret_cast<const void *>(part_partition_pipe_kernel<false, kMaxWin / kThreads>));
     if (s == EDPP_OK)
-      s = cuda_status(cudaFuncSetAttribute(part_partition_pipe_kernel<true>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           static_cast<int>(part_pipe_smem(kMaxWin))));
+      s = pipe(reinterpret_cast<const void *>(part_partition_pipe_kernel<true, kMaxWin / kThreads>));
     if (s == EDPP_OK) s = set_smem(part_fetch_kernel);
     st[d] = s;
   });
@@ -543,14 +628,17 @@ int launch_partition(const int32_t *loc, const int32_t *in, int64_t n, int log_w
   unsigned *fault = fault_word();
   if (!fault) return EDPP_ECUDA;
   const size_t smem = part_pipe_smem(nwin);
-  int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, part_partition_pipe_kernel<kScatter>,
-                                                    kThreads, smem) != cudaSuccess)
-    return EDPP_ECUDA;
-  const int64_t blocks = min64(tiles, static_cast<int64_t>(device_sm_count()) * max64(per_sm, 1));
-  part_partition_pipe_kernel<kScatter><<<static_cast<unsigned>(blocks), kThreads, smem, st>>>(
-      loc, in, n, log_w, nwin, fill, pairs, kDefaultWaitNs, fault);
-  return launch_status();
+  auto run = [&](auto kernel) -> int {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, smem) != cudaSuccess)
+      return EDPP_ECUDA;
+    const int64_t blocks = min64(tiles, static_cast<int64_t>(device_sm_count()) * max64(per_sm, 1));
+    kernel<<<static_cast<unsigned>(blocks), kThreads, smem, st>>>(loc, in, n, log_w, nwin, fill,
+                                                                  pairs, kDefaultWaitNs, fault);
+    return launch_status();
+  };
+  if (nwin <= kThreads) return run(part_partition_pipe_kernel<kScatter, 1>);
+  return run(part_partition_pipe_kernel<kScatter, kMaxWin / kThreads>);
 }
 
 template <bool kScatter>
@@ -728,12 +816,15 @@ __global__ void __launch_bounds__(1024)
 // window's cursor.  The tiles ("slots") are either the flat range [0, *total)
 // cut into kTile pairs, or, with region_log > 0, each region
 // [r << region_log, region_end[r]) cut the same way (slots past a region's
-// end are empty).  Persistent blocks take slots blockIdx, +gridDim, ...; the
-// slot after next is copied into shared memory by TMA while the current one
-// is processed, so loads stay in flight through the block's grouping work.
-// A slot whose fine windows span at most kRefineSpan is grouped in shared
-// memory (the landed input buffer is reused as the staging area) and written
-// as one run per window; a wider one (skewed keys) appends pair by pair.
+// end are empty).  Either way the pairs are ordered by coarse window
+// (pair.x >> coarse_log), so a slot's fine windows lie in the coarse windows
+// of its first and last pair.  Persistent blocks take slots blockIdx,
+// +gridDim, ...; the slot after next is copied into shared memory by TMA
+// while the current one is processed, so loads stay in flight through the
+// block's grouping work.  A slot whose fine windows span at most kRefineSpan
+// is grouped in shared memory (the landed input buffer is reused as the
+// staging area) and written as one run per window; a wider one (skewed keys)
+// appends pair by pair.
 constexpr int kRefineSpan = 512;
 constexpr int kRefineBlocksPerSm = 3;
 
@@ -764,19 +855,21 @@ __device__ __forceinline__ void refine_issue(const int2 *src, int64_t lo, int64_
 __global__ void __launch_bounds__(kThreads, kRefineBlocksPerSm)
     win_refine_kernel(const int2 *__restrict__ src, const uint32_t *__restrict__ total_p,
                       const uint32_t *__restrict__ region_end, int region_log, int fine_log,
-                      int64_t slots, uint32_t *__restrict__ fill, int2 *__restrict__ dst,
-                      uint64_t timeout_ns, unsigned *fault) {
+                      int coarse_log, int64_t slots, uint32_t *__restrict__ fill,
+                      int2 *__restrict__ dst, uint64_t timeout_ns, unsigned *fault) {
   extern __shared__ __align__(16) unsigned char smem[];
   int2 *bufs = reinterpret_cast<int2 *>(smem);  // [2][kTile]
   uint32_t *scnt = reinterpret_cast<uint32_t *>(bufs + 2 * kTile);
   uint32_t *soff = scnt + kRefineSpan;
   uint32_t *sgb = soff + kRefineSpan;
   __shared__ alignas(8) uint64_t bar[2];
-  __shared__ uint32_t s_warp[16];
-  __shared__ int s_lo, s_hi;
+  __shared__ uint32_t s_total;
   const int t = threadIdx.x;
   const int64_t G = gridDim.x;
+  const int fan = coarse_log - fine_log;
+  for (int i = t; i < kRefineSpan; i += kThreads) scnt[i] = 0;
   if (t == 0) {
+    s_total = 0;
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
     fence_mbar_init();
@@ -790,7 +883,6 @@ __global__ void __launch_bounds__(kThreads, kRefineBlocksPerSm)
     }
   }
   __syncthreads();
-  const unsigned lt = lanemask_lt();
   uint32_t phase = 0;  // bit b: parity of bar[b]'s next completion
   int b = 0;
   int64_t slot = blockIdx.x;
@@ -801,76 +893,64 @@ __global__ void __launch_bounds__(kThreads, kRefineBlocksPerSm)
     int2 *buf = bufs + b * kTile;
     if (lo < hi) {  // block-uniform
       const uint32_t cnt = static_cast<uint32_t>(hi - lo);
+      const uint32_t even = cnt & ~1u;  // pairs in the bulk copy; an odd last one is read from src
       bool bad = false;
-      if (cnt & ~1u) {
+      if (even) {
         bad = !mbar_wait_bounded(&bar[b], (phase >> b) & 1u, timeout_ns, fault);
         phase ^= 1u << b;
       }
-      if (t == 0) {
-        if (cnt & 1u) buf[cnt - 1] = src[hi - 1];
-        s_lo = INT_MAX;
-        s_hi = -1;
+      int wlo = 0, span = 0;
+      if (!bad) {
+        const int2 first = even ? buf[0] : src[lo];
+        const int2 last = (cnt & 1u) ? src[hi - 1] : buf[cnt - 1];
+        const int c0 = first.x >> coarse_log, c1 = last.x >> coarse_log;
+        wlo = c0 << fan;
+        span = (c1 - c0 + 1) << fan;
       }
-      for (int i = t; i < kRefineSpan; i += kThreads) scnt[i] = 0;
-      if (__syncthreads_or(bad)) {
-        failed = true;
-        break;
-      }
+      const bool grouped = span <= kRefineSpan;  // uniform unless bad
       int2 pr[kPer];
       int fid[kPer];
-      int my_lo = INT_MAX, my_hi = -1;
 #pragma unroll
       for (int k = 0; k < kPer / 2; ++k) {
         const uint32_t j = static_cast<uint32_t>(k * kThreads + t) * 2u;
         int4 q = make_int4(0, 0, 0, 0);
-        if (j + 1 < cnt) q = *reinterpret_cast<const int4 *>(buf + j);
-        else if (j < cnt) { const int2 a = buf[j]; q.x = a.x; q.y = a.y; }
+        if (j < even) {
+          if (!bad) q = *reinterpret_cast<const int4 *>(buf + j);
+        } else if (j < cnt) {
+          const int2 a = src[lo + j];
+          q.x = a.x;
+          q.y = a.y;
+        }
         pr[2 * k] = make_int2(q.x, q.y);
         pr[2 * k + 1] = make_int2(q.z, q.w);
-        fid[2 * k] = j < cnt ? (q.x >> fine_log) : -1;
-        fid[2 * k + 1] = j + 1 < cnt ? (q.z >> fine_log) : -1;
+        fid[2 * k] = (j < cnt && !bad) ? (q.x >> fine_log) - wlo : -1;
+        fid[2 * k + 1] = (j + 1 < cnt && !bad) ? (q.z >> fine_log) - wlo : -1;
       }
-#pragma unroll
-      for (int e = 0; e < kPer; ++e)
-        if (fid[e] >= 0) {
-          my_lo = min(my_lo, fid[e]);
-          my_hi = max(my_hi, fid[e]);
-        }
-#pragma unroll
-      for (int m = 16; m >= 1; m >>= 1) {
-        my_lo = min(my_lo, __shfl_xor_sync(0xffffffffu, my_lo, m));
-        my_hi = max(my_hi, __shfl_xor_sync(0xffffffffu, my_hi, m));
-      }
-      if ((t & 31) == 0) {
-        atomicMin(&s_lo, my_lo);
-        atomicMax(&s_hi, my_hi);
-      }
-      __syncthreads();  // also: every read of buf is done
-      const int wlo = s_lo, span = s_hi - s_lo + 1;
-      if (span > kRefineSpan) {  // skewed slot: one cursor claim per pair
+      // fid[e] becomes (window << 12) | rank, or -1 (kTile = 2^12 ranks)
+      if (grouped) {
 #pragma unroll
         for (int e = 0; e < kPer; ++e)
-          if (fid[e] >= 0) dst[atomicAdd(&fill[fid[e]], 1u)] = pr[e];
+          if (fid[e] >= 0) fid[e] = (fid[e] << 12) | static_cast<int>(atomicAdd(&scnt[fid[e]], 1u));
+      }
+      if (__syncthreads_or(bad)) {  // A: ranks complete; every read of buf done
+        failed = true;
+        break;
+      }
+      if (!grouped) {  // skewed slot: one cursor claim per pair
+#pragma unroll
+        for (int e = 0; e < kPer; ++e)
+          if (fid[e] >= 0) dst[atomicAdd(&fill[wlo + fid[e]], 1u)] = pr[e];
       } else {
-        int rank[kPer];
-#pragma unroll
-        for (int e = 0; e < kPer; ++e) {
-          fid[e] = fid[e] >= 0 ? fid[e] - wlo : -1;
-          rank[e] = rank_in_window(fid[e], scnt, lt);
-        }
-        __syncthreads();
-        const uint32_t total = block_scan_counts(scnt, soff, span, s_warp);
-        // run start minus staging offset; the first claim's round trip
-        // overlaps the staging writes
-        const uint32_t c0 = t < span ? scnt[t] : 0u;
-        const uint32_t g0 = c0 ? atomicAdd(&fill[wlo + t], c0) : 0u;
-        for (int i = t + kThreads; i < span; i += kThreads)
-          if (scnt[i]) sgb[i] = atomicAdd(&fill[wlo + i], scnt[i]) - soff[i];
+        uint32_t g[kRefineSpan / kThreads], o[kRefineSpan / kThreads];
+        claim_runs<kRefineSpan / kThreads, kThreads>(scnt, soff, span, fill + wlo, &s_total, g, o);
+        __syncthreads();  // B
+        const uint32_t total = s_total;
 #pragma unroll
         for (int e = 0; e < kPer; ++e)
-          if (fid[e] >= 0) buf[soff[fid[e]] + rank[e]] = pr[e];
-        if (c0) sgb[t] = g0 - soff[t];
-        __syncthreads();
+          if (fid[e] >= 0) buf[soff[fid[e] >> 12] + (fid[e] & (kTile - 1))] = pr[e];
+        publish_run_bases<kRefineSpan / kThreads, kThreads>(sgb, span, g, o);
+        __syncthreads();  // C
+        if (t == 0) s_total = 0;
         for (uint32_t q = t; q < total; q += kThreads) {
           const int2 p = buf[q];
           dst[sgb[(p.x >> fine_log) - wlo] + q] = p;
@@ -961,7 +1041,10 @@ __global__ void __launch_bounds__(kWinThreads)
 
 // Gather fetch: one block per fine window f of in[]; the window is loaded
 // once into shared memory, and each pair {loc, i} of the window becomes
-// {i, in[loc]}, appended to the coarse window of i (cursors cfill2).
+// {i, in[loc]}, appended to the coarse window of i (cursors cfill2).  The
+// window's pairs go in sub-tiles of kTile; each sub-tile's pairs are loaded
+// into registers while the previous one is grouped (the first while the
+// window lands).
 constexpr int kFetchThreads = 512;
 constexpr int kFetchPer = kTile / kFetchThreads;  // 8 pairs per thread per sub-tile
 
@@ -977,13 +1060,21 @@ __global__ void __launch_bounds__(kFetchThreads)
   uint32_t *scnt = reinterpret_cast<uint32_t *>(stage + kTile);
   uint32_t *soff = scnt + C;
   uint32_t *sgb = soff + C;
-  __shared__ uint32_t s_warp[kFetchThreads / 32 + 1];
+  __shared__ uint32_t s_total;
   __shared__ alignas(8) uint64_t bar;
   const int f = blockIdx.x, t = threadIdx.x;
   const int64_t base = static_cast<int64_t>(f) << fine_log;
   const int len = static_cast<int>(min64(W, n - base));
   const int64_t lo = start[f], hi = start[f + 1];
   if (lo >= hi) return;  // block-uniform
+  int2 nxt[kFetchPer];
+  auto load = [&](int64_t c0) {
+#pragma unroll
+    for (int e = 0; e < kFetchPer; ++e) {
+      const int64_t j = c0 + static_cast<int64_t>(e) * kFetchThreads + t;
+      nxt[e] = j < hi ? __ldcs(pairs + j) : make_int2(0, 0);
+    }
+  };
   // the window by one bulk copy (16-byte multiple), the rest by plain loads
   const uint32_t bulk = vec_in ? (static_cast<uint32_t>(len) * 4u) & ~15u : 0u;
   if (t == 0 && bulk) {
@@ -992,28 +1083,41 @@ __global__ void __launch_bounds__(kFetchThreads)
     mbar_arrive_expect_tx(&bar, bulk);
     tma_load_1d(win, in + base, bulk, &bar);
   }
+  load(lo);
   for (int e = static_cast<int>(bulk / 4) + t; e < len; e += kFetchThreads) win[e] = in[base + e];
+  for (int i = t; i < C; i += kFetchThreads) scnt[i] = 0;
+  if (t == 0) s_total = 0;
   __syncthreads();  // barrier initialised before anyone waits on it
   if (bulk && __syncthreads_or(!mbar_wait_bounded(&bar, 0, timeout_ns, fault))) return;
-  const unsigned lt = lanemask_lt();
   for (int64_t c0 = lo; c0 < hi; c0 += kTile) {
-    for (int i = t; i < C; i += kFetchThreads) scnt[i] = 0;
-    __syncthreads();  // also: window loaded, previous tile's stage consumed
+    int2 a[kFetchPer];
+#pragma unroll
+    for (int e = 0; e < kFetchPer; ++e) a[e] = nxt[e];
+    if (c0 + kTile < hi) load(c0 + kTile);
     int2 pr[kFetchPer];
     int w[kFetchPer], rank[kFetchPer];
 #pragma unroll
     for (int e = 0; e < kFetchPer; ++e) {
-      const int64_t j = c0 + static_cast<int64_t>(e) * kFetchThreads + t;
-      const bool valid = j < hi;
-      const int2 a = valid ? pairs[j] : make_int2(0, 0);
-      pr[e] = make_int2(a.y, valid ? win[a.x - base] : 0);  // {i, value}
-      w[e] = valid ? (a.y >> coarse_log) : -1;
-      rank[e] = rank_in_window(w[e], scnt, lt);
+      const bool valid = c0 + static_cast<int64_t>(e) * kFetchThreads + t < hi;
+      pr[e] = make_int2(a[e].y, valid ? win[a[e].x - base] : 0);  // {i, value}
+      w[e] = valid ? (a[e].y >> coarse_log) : -1;
+      rank[e] = valid ? static_cast<int>(atomicAdd(&scnt[w[e]], 1u)) : -1;
     }
-    __syncthreads();
-    flush_runs<kFetchPer, kFetchThreads>(pr, w, rank, C, coarse_log, scnt, soff, sgb, s_warp, stage,
-                                         cfill2, dst);
-    __syncthreads();
+    __syncthreads();  // A
+    uint32_t g[1], o[1];
+    claim_runs<1, kFetchThreads>(scnt, soff, C, cfill2, &s_total, g, o);
+    __syncthreads();  // B
+    const uint32_t total = s_total;
+#pragma unroll
+    for (int e = 0; e < kFetchPer; ++e)
+      if (w[e] >= 0) stage[soff[w[e]] + rank[e]] = pr[e];
+    publish_run_bases<1, kFetchThreads>(sgb, C, g, o);
+    __syncthreads();  // C
+    if (t == 0) s_total = 0;
+    for (uint32_t q = t; q < total; q += kFetchThreads) {
+      const int2 p = stage[q];
+      dst[sgb[p.x >> coarse_log] + q] = p;
+    }
   }
 }
 
@@ -1114,7 +1218,7 @@ int tiled_run(const int32_t *in, int32_t *out, int64_t n, const int32_t *loc, in
   if (!fault) return EDPP_ECUDA;
   const int64_t rblocks = static_cast<int64_t>(sms) * kRefineBlocksPerSm;
   win_refine_kernel<<<static_cast<unsigned>(min64(tiles, rblocks)), kThreads, refine_smem(), st>>>(
-      pa, start + p.F, nullptr, 0, p.fine_log, tiles, fill, pb, kDefaultWaitNs, fault);
+      pa, start + p.F, nullptr, 0, p.fine_log, p.coarse_log, tiles, fill, pb, kDefaultWaitNs, fault);
   if (kScatter) {
     win_apply_kernel<<<static_cast<unsigned>(p.F), kWinThreads, apply_smem(p.fine_log), st>>>(
         pb, start, nullptr, p.fine_log, n, out, aligned16(out));
@@ -1123,7 +1227,8 @@ int tiled_run(const int32_t *in, int32_t *out, int64_t n, const int32_t *loc, in
         pb, start, in, n, p.fine_log, p.coarse_log, p.C, cfill2, pa, vec_in, kDefaultWaitNs, fault);
     const int64_t rtiles = static_cast<int64_t>(p.C) << (p.coarse_log - 12);
     win_refine_kernel<<<static_cast<unsigned>(min64(rtiles, rblocks)), kThreads, refine_smem(), st>>>(
-        pa, nullptr, cfill2, p.coarse_log, p.fine_log, rtiles, fill2, pb, kDefaultWaitNs, fault);
+        pa, nullptr, cfill2, p.coarse_log, p.fine_log, p.coarse_log, rtiles, fill2, pb,
+        kDefaultWaitNs, fault);
     win_apply_kernel<<<static_cast<unsigned>(p.F), kWinThreads, apply_smem(p.fine_log), st>>>(
         pb, nullptr, fill2, p.fine_log, n, out, aligned16(out));
   }
