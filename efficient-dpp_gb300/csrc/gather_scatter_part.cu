@@ -307,7 +307,7 @@ __global__ void __launch_bounds__(kThreads)
 // from global memory by the thread that ranks them.  nwin <= MAXPER * kThreads.
 // Same output as part_partition_kernel.
 template <bool kScatter, int MAXPER>
-__global__ void __launch_bounds__(kThreads, 2)
+__global__ void __launch_bounds__(kThreads, MAXPER == 1 ? 3 : 2)
     part_partition_pipe_kernel(const int32_t *__restrict__ loc, const int32_t *__restrict__ in,
                                int64_t n, int log_w, int nwin, uint32_t *__restrict__ fill,
                                int2 *__restrict__ pairs, uint64_t timeout_ns, unsigned *fault) {
@@ -358,7 +358,7 @@ __global__ void __launch_bounds__(kThreads, 2)
       phase ^= 1u << b;
     }
     int2 pr[kPer];
-    int w[kPer], rank[kPer];
+    int wr[kPer];  // (window << 12) | rank, or -1 (kTile = 2^12 ranks)
 #pragma unroll
     for (int k = 0; k < kPer / 4; ++k) {
       const int i0 = (k * kThreads + t) * 4;
@@ -384,9 +384,9 @@ __global__ void __launch_bounds__(kThreads, 2)
       for (int q = 0; q < 4; ++q) {
         const int e = 4 * k + q;
         const bool valid = (i0 + q < count) && ls[q] >= 0 && static_cast<int64_t>(ls[q]) < n;
-        w[e] = valid ? (ls[q] >> log_w) : -1;
+        const int w = ls[q] >> log_w;
         pr[e] = make_int2(ls[q], kScatter ? vs[q] : static_cast<int32_t>(base + i0 + q));
-        rank[e] = valid ? static_cast<int>(atomicAdd(&scnt[w[e]], 1u)) : -1;
+        wr[e] = valid ? (w << 12) | static_cast<int>(atomicAdd(&scnt[w], 1u)) : -1;
       }
     }
     if (__syncthreads_or(bad)) {  // A: counts complete; every read of buf done
@@ -400,7 +400,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     int2 *stage = reinterpret_cast<int2 *>(buf);
 #pragma unroll
     for (int e = 0; e < kPer; ++e)
-      if (w[e] >= 0) stage[soff[w[e]] + rank[e]] = pr[e];
+      if (wr[e] >= 0) stage[soff[wr[e] >> 12] + (wr[e] & (kTile - 1))] = pr[e];
     publish_run_bases<MAXPER, kThreads>(sgb, nwin, g, o);
     __syncthreads();  // C
     if (t == 0) s_total = 0;
