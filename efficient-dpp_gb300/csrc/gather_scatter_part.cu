@@ -1283,10 +1283,11 @@ int edpp_scatter_i32_tiled(const int32_t *in, int32_t *out, int64_t length, cons
 }
 
 int edpp_gather_prefers_direct(int64_t length) {
-  // A gather whose source is at most ~2.5x L2 keeps enough of it in L2 that
-  // the direct random sweep wins (measured: 2^26 int32 1.0-1.2 ms direct,
-  // 1.36 ms tiled; 2^28 5.6-6.0 ms direct, 5.2-5.3 ms tiled).
-  return static_cast<double>(length) * 4.0 <= 2.5 * static_cast<double>(edpp::device_l2_bytes());
+  // A gather whose source is at most ~1.5x L2 keeps enough of it in L2 that
+  // the direct random sweep wins (measured, int32 permutations: 2^25 0.49 ms
+  // direct against 0.59 ms tiled; 2^26 1.21 against 1.10; 2^27 2.79
+  // against 2.11; 2^28 5.6-6.0 against 4.3).
+  return static_cast<double>(length) * 4.0 <= 1.5 * static_cast<double>(edpp::device_l2_bytes());
 }
 
 }  // extern "C"
