@@ -173,6 +173,16 @@ __global__ void __launch_bounds__(THREADS)
     }
   }
   for (int i = tid; i < C::kWarps * buckets; i += THREADS) cnt16[i] = 0;
+  // This thread's buckets for the per-bucket combine below; the first
+  // kHisPre of their global run starts (his[b*T + t], one 32-byte sector
+  // each) are loaded now, so the round trip overlaps the tile's ranking.
+  const int per = (buckets + THREADS - 1) / THREADS;
+  const int b_lo = min(buckets, tid * per), b_hi = min(buckets, b_lo + per);
+  constexpr int kHisPre = THREADS >= 512 ? 2 : 4;  // 512 threads serve up to 1024 buckets
+  int32_t his_pre[kHisPre];
+#pragma unroll
+  for (int k = 0; k < kHisPre; ++k)
+    his_pre[k] = b_lo + k < b_hi ? __ldg(his + static_cast<int64_t>(b_lo + k) * tiles + t) : 0;
   if (bulk_elems) {
     if (!mbar_wait_bounded(&bar, 0, timeout_ns, fault)) return;
   }
@@ -251,8 +261,6 @@ __global__ void __launch_bounds__(THREADS)
   // -- per bucket: exclusive prefix over warps, tile count, tile offsets --
   // Thread-consecutive buckets so the block-wide scan over buckets is a
   // per-thread serial scan plus one warp/ block combine.
-  const int per = (buckets + THREADS - 1) / THREADS;
-  const int b_lo = min(buckets, tid * per), b_hi = min(buckets, b_lo + per);
   int32_t my_total = 0;
   for (int b = b_lo; b < b_hi; ++b) {
     int32_t run = 0;
@@ -287,10 +295,20 @@ __global__ void __launch_bounds__(THREADS)
   }
   __syncthreads();
   int32_t run = s_wsum[w] + (incl - my_total);
-  for (int b = b_lo; b < b_hi; ++b) {
+#pragma unroll
+  for (int k = 0; k < kHisPre; ++k) {
+    const int b = b_lo + k;
+    if (b < b_hi) {
+      const int32_t c = toff[b];
+      toff[b] = run;
+      // First output index of bucket b from this tile, minus its tile offset.
+      gofs[b] = his_pre[k] - run;
+      run += c;
+    }
+  }
+  for (int b = b_lo + kHisPre; b < b_hi; ++b) {
     const int32_t c = toff[b];
     toff[b] = run;
-    // First output index of bucket b from this tile, minus its tile offset.
     gofs[b] = his[static_cast<int64_t>(b) * tiles + t] - run;
     run += c;
   }
