@@ -39,6 +39,7 @@ namespace {
 constexpr int kTile = 8192;
 constexpr int kMaxBuckets = 4096;
 constexpr int kHistThreads = 512;
+constexpr int kDirectBuckets = 2;  // up to this many buckets the scatter writes from registers
 
 __device__ __forceinline__ unsigned lanemask_lt() {
   unsigned m;
@@ -313,6 +314,31 @@ __global__ void __launch_bounds__(THREADS)
     run += c;
   }
   __syncthreads();
+
+  // -- two buckets: each warp's lanes of one bucket hold consecutive output
+  // slots, so every store instruction covers at most two contiguous
+  // stretches; write from registers, skipping the shared-memory re-layout
+  // (2^28 pairs: 1.21 -> 1.11 ms; at 4 buckets even, at 8 and more slower,
+  // the stores' sectors being only partly filled) --
+  if (buckets <= kDirectBuckets) {
+#pragma unroll
+    for (int it = 0; it < C::kIters; ++it) {
+      const int pos = w * C::kSeg + it * 32 + lane;
+      if (pos < count) {
+        const int b = static_cast<int>((static_cast<unsigned>(kk[it]) >> shift) & mask);
+        const int r = static_cast<int>((rk[it >> 1] >> ((it & 1) * 16)) & 0xffffu);
+        const int64_t o =
+            static_cast<int64_t>(gofs[b]) + toff[b] + cnt16[w * buckets + b] + r;
+        if (LAYOUT == EDPP_KVS_AOS) {
+          reinterpret_cast<int2 *>(keys_out)[o] = make_int2(kk[it], vv[it]);
+        } else {
+          keys_out[o] = kk[it];
+          if (LAYOUT == EDPP_KVS_SOA) vals_out[o] = vv[it];
+        }
+      }
+    }
+    return;
+  }
 
   // -- re-lay the tile out in bucket order (stable) --
 #pragma unroll
