@@ -106,24 +106,239 @@ __device__ void block_exclusive_scan_inplace(int32_t *p, int64_t m, int32_t *wsu
   __syncthreads();
 }
 
+// ---- tile task bodies, shared by the work-queue kernel and the per-kind kernels ----
+
+struct TaskIO {
+  const int32_t *in0, *in1;
+  int32_t *out0, *out1;
+  char *state;
+  uint64_t timeout_ns;
+  unsigned *fault, *abort_flag;
+  bool tma;
+  int num_segs;
+};
+
+// A task's segment and tile must lie inside the plan's tables (a workspace
+// without an uploaded plan holds garbage): otherwise record EDPP_FAULT_PLAN
+// and skip the task.  Block-uniform.
+__device__ __forceinline__ bool task_in_plan(const DevTask &task, const DevSeg *segs,
+                                             const TaskIO &io, DevSeg &seg) {
+  if (task.seg < 0 || task.seg >= io.num_segs) {
+    if (threadIdx.x == 0) raise_fault(io.fault, EDPP_FAULT_PLAN);
+    return false;
+  }
+  seg = segs[task.seg];
+  if (task.tile < 0 || task.tile >= seg.tiles) {
+    if (threadIdx.x == 0) raise_fault(io.fault, EDPP_FAULT_PLAN);
+    return false;
+  }
+  return true;
+}
+
+// Exclusive scan of one tile with a decoupled look-back over the segment's
+// own tile states.  `released()` runs (every thread) once no other task can
+// wait on this one any more: after the inclusive prefix is published.
+template <typename F>
+__device__ __forceinline__ void scan_tile_task(const DevSeg &seg, int tile, const TaskIO &io,
+                                               int32_t *tile_smem, TS32::Shared &sh,
+                                               uint64_t *bar, uint32_t &phase, F released) {
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  const int64_t tile_base = static_cast<int64_t>(tile) * kTile;
+  const int count = static_cast<int>(min64(kTile, seg.len - tile_base));
+  const int64_t gbase = seg.off + tile_base;
+  LookbackState<int32_t> st;
+  st.bind(io.state + seg.state, seg.tiles);
+  const bool tma_ok = io.tma && ((gbase & 3) == 0);  // 16-byte aligned tile start
+  const uint32_t bulk =
+      stage_tile<int32_t, kTile, kThreads>(tile_smem, io.in0 + gbase, count, tma_ok, bar);
+  if (bulk) {
+    if (!mbar_wait_bounded(bar, phase, io.timeout_ns, io.fault)) atomicOr(io.abort_flag, 1u);
+    phase ^= 1u;
+  }
+  __syncthreads();
+  Chunk<int32_t> c[kChunks];
+  int32_t wex[kChunks];
+  TS32::phase1(tile_smem, c, wex, sh);
+  __syncthreads();
+  if (w == 0) {
+    const int32_t agg = TS32::phase2_warp0(sh, lane);
+    int32_t prefix = 0;
+    bool ok = true;
+    if (tile == 0) {
+      if (lane == 0) st.publish(0, kFlagIncl, agg);
+    } else {
+      prefix = lookback_warp<int32_t>(st, tile, agg, lane, io.timeout_ns, io.fault, io.abort_flag,
+                                      ok);
+    }
+    if (lane == 0) sh.prefix = ok ? prefix : 0;
+  }
+  released();
+  __syncthreads();
+  TS32::phase3<false>(c, wex, sh, sh.prefix);
+  TS32::store(io.out0, gbase, count, c, (reinterpret_cast<uintptr_t>(io.out0 + gbase) & 15) == 0);
+}
+
+// Permutation gather of one tile, indices local to the segment.
+__device__ __forceinline__ void gather_tile_task(const DevSeg &seg, int tile, const TaskIO &io) {
+  const int t = threadIdx.x;
+  const int64_t tile_base = static_cast<int64_t>(tile) * kTile;
+  const int count = static_cast<int>(min64(kTile, seg.len - tile_base));
+  const int64_t gbase = seg.off + tile_base;
+  const int32_t *src = io.in0 + seg.off;
+#pragma unroll
+  for (int k = 0; k < kTile / kThreads; k += 4) {
+    int v[4], idx[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int i = (k + q) * kThreads + t;
+      idx[q] = i < count ? io.in1[gbase + i] : -1;
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) v[q] = (idx[q] >= 0 && idx[q] < seg.len) ? __ldg(src + idx[q]) : 0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int i = (k + q) * kThreads + t;
+      if (idx[q] >= 0 && idx[q] < seg.len) io.out0[gbase + i] = v[q];
+    }
+  }
+}
+
+// Bucket counts of one split tile -> column `tile` of the segment's
+// bucket-major histogram his[b*T + tile].  cnt: shared, >= seg.buckets.
+__device__ __forceinline__ void hist_tile_task(const DevSeg &seg, int tile, const TaskIO &io,
+                                               uint32_t *cnt) {
+  const int t = threadIdx.x;
+  const int64_t tile_base = static_cast<int64_t>(tile) * kTile;
+  const int count = static_cast<int>(min64(kTile, seg.len - tile_base));
+  const int64_t gbase = seg.off + tile_base;
+  const unsigned mask = static_cast<unsigned>(seg.buckets - 1);
+  for (int b = t; b < seg.buckets; b += kThreads) cnt[b] = 0;
+  __syncthreads();
+  for (int i0 = 0; i0 < kTile; i0 += kThreads) {
+    const int i = i0 + t;
+    if (i < count) atomicAdd(&cnt[static_cast<unsigned>(io.in0[gbase + i]) & mask], 1u);
+  }
+  __syncthreads();
+  int32_t *his = reinterpret_cast<int32_t *>(io.state + seg.state);
+  for (int b = t; b < seg.buckets; b += kThreads)
+    his[static_cast<int64_t>(b) * seg.tiles + tile] = static_cast<int32_t>(cnt[b]);
+}
+
+// Stable key/value scatter of one split tile; the segment's histogram is
+// scanned (his[b*T + t] = first output index of bucket b from tile t).
+// Same ranking as split.cu.
+__device__ __forceinline__ void split_tile_task(const DevSeg &seg, int tile, const TaskIO &io,
+                                                BatchSmem &sm) {
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  const unsigned lt = lanemask_lt_b();
+  const int64_t tile_base = static_cast<int64_t>(tile) * kTile;
+  const int count = static_cast<int>(min64(kTile, seg.len - tile_base));
+  const int64_t gbase = seg.off + tile_base;
+  const unsigned mask = static_cast<unsigned>(seg.buckets - 1);
+  const int B = seg.buckets;
+  const int32_t *his = reinterpret_cast<const int32_t *>(io.state + seg.state);
+  for (int i = t; i < count; i += kThreads) {
+    sm.split.keys[i] = io.in0[gbase + i];
+    sm.split.vals[i] = io.in1[gbase + i];
+  }
+  for (int i = t; i < kWarps * B; i += kThreads) sm.split.cnt16[i] = 0;
+  __syncthreads();
+  uint16_t *my = sm.split.cnt16 + w * B;
+  const int kbits = 31 - __clz(B);
+  int32_t kk[kIters], vv[kIters];
+  uint32_t rk[kIters / 2];
+#pragma unroll
+  for (int it = 0; it < kIters; ++it) {
+    const int pos = w * kSeg + it * 32 + lane;
+    const bool valid = pos < count;
+    const int32_t key = valid ? sm.split.keys[pos] : 0;
+    const int32_t val = valid ? sm.split.vals[pos] : 0;
+    const int b = valid ? static_cast<int>(static_cast<unsigned>(key) & mask) : -1;
+    const unsigned vmask = __ballot_sync(0xffffffffu, valid);
+    unsigned peers;
+    if (kbits <= 5) {
+      peers = match_low_bits(static_cast<unsigned>(b), kbits, vmask);
+    } else {  // one leader lane per bucket, 5 votes on its lane number
+      if (valid) sm.split.last[w * B + b] = static_cast<uint8_t>(lane);
+      __syncwarp();
+      peers = match_low_bits(valid ? sm.split.last[w * B + b] : 0u, 5, vmask);
+    }
+    const unsigned lower = peers & lt;
+    const uint16_t before = valid ? my[b] : 0;
+    __syncwarp();
+    if (valid && lower == 0u) my[b] = static_cast<uint16_t>(before + __popc(peers));
+    __syncwarp();
+    kk[it] = key;
+    vv[it] = val;
+    const uint32_t r = static_cast<uint32_t>(before + __popc(lower));
+    if (it & 1) rk[it >> 1] |= r << 16;
+    else rk[it >> 1] = r;
+  }
+  __syncthreads();
+  // per bucket: exclusive prefix over warps; tile counts; tile offsets
+  if (t < 32) {
+    int32_t run_total = 0;
+    for (int b0 = 0; b0 < B; b0 += 32) {
+      const int b = b0 + lane;
+      int32_t tot = 0;
+      if (b < B) {
+        for (int ww = 0; ww < kWarps; ++ww) {
+          const int32_t c = sm.split.cnt16[ww * B + b];
+          sm.split.cnt16[ww * B + b] = static_cast<uint16_t>(tot);
+          tot += c;
+        }
+      }
+      int32_t incl = tot;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const int32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += y;
+      }
+      if (b < B) {
+        const int32_t off = run_total + incl - tot;
+        sm.split.toff[b] = off;
+        sm.split.gofs[b] = __ldcg(his + static_cast<int64_t>(b) * seg.tiles + tile) - off;
+      }
+      run_total += __shfl_sync(0xffffffffu, incl, 31);
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int it = 0; it < kIters; ++it) {
+    const int pos = w * kSeg + it * 32 + lane;
+    if (pos < count) {
+      const int b = static_cast<int>(static_cast<unsigned>(kk[it]) & mask);
+      const int r = static_cast<int>((rk[it >> 1] >> ((it & 1) * 16)) & 0xffffu);
+      const int s = sm.split.toff[b] + sm.split.cnt16[w * B + b] + r;
+      sm.split.keys[s] = kk[it];
+      sm.split.vals[s] = vv[it];
+    }
+  }
+  __syncthreads();
+  for (int s = t; s < count; s += kThreads) {
+    const int32_t key = sm.split.keys[s];
+    const int b = static_cast<int>(static_cast<unsigned>(key) & mask);
+    const int64_t o = seg.off + sm.split.gofs[b] + s;
+    io.out0[o] = key;
+    io.out1[o] = sm.split.vals[s];
+  }
+}
+
+// ---- QUEUE schedule: one persistent launch over the work queue ----
 __global__ void __launch_bounds__(kThreads, 3)
     batch_kernel(const DevSeg *__restrict__ segs, const DevTask *__restrict__ tasks, int num_tasks,
-                 const int32_t *__restrict__ in0, const int32_t *__restrict__ in1,
-                 int32_t *__restrict__ out0, int32_t *__restrict__ out1, char *state,
-                 Ctrl *ctrl, unsigned long long *ticket, unsigned *abort_flag, bool tma,
-                 uint64_t timeout_ns, unsigned *fault) {
+                 TaskIO io, Ctrl *ctrl, unsigned long long *ticket) {
   __shared__ BatchSmem sm;
   __shared__ alignas(8) uint64_t bar;
   __shared__ int s_task;
   __shared__ int s_flag;
-  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  const int t = threadIdx.x;
   if (t == 0) {
     mbar_init(&bar, 1);
     fence_mbar_init();
   }
   __syncthreads();
   uint32_t phase = 0;
-  const unsigned lt = lanemask_lt_b();
 
   // Thread 0 takes the next ticket early, once nothing can wait on the
   // current task any more: a SCAN tile after publishing its prefix, a SPLIT
@@ -146,78 +361,19 @@ __global__ void __launch_bounds__(kThreads, 3)
     const int task_id = s_task;
     if (task_id >= num_tasks) break;
     const DevTask task = tasks[task_id];
-    const DevSeg seg = segs[task.seg];
-    const int64_t tile_base = static_cast<int64_t>(task.tile) * kTile;
-    const int count = static_cast<int>(min64(kTile, seg.len - tile_base));
-    const int64_t gbase = seg.off + tile_base;
-
+    DevSeg seg;
+    if (!task_in_plan(task, segs, io, seg)) {
+      if (t == 0) atomicOr(io.abort_flag, 1u);
+      break;  // block-uniform; the abort flag releases any waiting block
+    }
     if (task.kind == kTaskScan) {
-      // ---- exclusive scan tile with look-back inside the segment ----
-      LookbackState<int32_t> st;
-      st.bind(state + seg.state, seg.tiles);
-      const bool tma_ok = tma && ((gbase & 3) == 0);  // 16-byte aligned tile start
-      const uint32_t bulk =
-          stage_tile<int32_t, kTile, kThreads>(sm.scan.tile, in0 + gbase, count, tma_ok, &bar);
-      if (bulk) {
-        if (!mbar_wait_bounded(&bar, phase, timeout_ns, fault)) atomicOr(abort_flag, 1u);
-        phase ^= 1u;
-      }
-      __syncthreads();
-      Chunk<int32_t> c[kChunks];
-      int32_t wex[kChunks];
-      TS32::phase1(sm.scan.tile, c, wex, sm.scan.sh);
-      __syncthreads();
-      if (w == 0) {
-        const int32_t agg = TS32::phase2_warp0(sm.scan.sh, lane);
-        int32_t prefix = 0;
-        bool ok = true;
-        if (task.tile == 0) {
-          if (lane == 0) st.publish(0, kFlagIncl, agg);
-        } else {
-          prefix = lookback_warp<int32_t>(st, task.tile, agg, lane, timeout_ns, fault, abort_flag,
-                                          ok);
-        }
-        if (lane == 0) sm.scan.sh.prefix = ok ? prefix : 0;
-      }
-      take_next();
-      __syncthreads();
-      TS32::phase3<false>(c, wex, sm.scan.sh, sm.scan.sh.prefix);
-      TS32::store(out0, gbase, count, c, (reinterpret_cast<uintptr_t>(out0 + gbase) & 15) == 0);
+      scan_tile_task(seg, task.tile, io, sm.scan.tile, sm.scan.sh, &bar, phase,
+                     [&] { take_next(); });
     } else if (task.kind == kTaskGather) {
-      // ---- permutation gather tile, indices local to the segment ----
       take_next();
-      const int32_t *src = in0 + seg.off;
-#pragma unroll
-      for (int k = 0; k < kTile / kThreads; k += 4) {
-        int v[4], idx[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int i = (k + q) * kThreads + t;
-          idx[q] = i < count ? in1[gbase + i] : -1;
-        }
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-          v[q] = (idx[q] >= 0 && idx[q] < seg.len) ? __ldg(src + idx[q]) : 0;
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int i = (k + q) * kThreads + t;
-          if (idx[q] >= 0 && idx[q] < seg.len) out0[gbase + i] = v[q];
-        }
-      }
+      gather_tile_task(seg, task.tile, io);
     } else if (task.kind == kTaskHist) {
-      // ---- bucket counts of a split tile ----
-      const unsigned mask = static_cast<unsigned>(seg.buckets - 1);
-      for (int b = t; b < seg.buckets; b += kThreads) sm.hist.cnt[b] = 0;
-      __syncthreads();
-      for (int i0 = 0; i0 < kTile; i0 += kThreads) {
-        const int i = i0 + t;
-        const bool valid = i < count;
-        if (valid) atomicAdd(&sm.hist.cnt[static_cast<unsigned>(in0[gbase + i]) & mask], 1u);
-      }
-      __syncthreads();
-      int32_t *his = reinterpret_cast<int32_t *>(state + seg.state);
-      for (int b = t; b < seg.buckets; b += kThreads)
-        his[static_cast<int64_t>(b) * seg.tiles + task.tile] = static_cast<int32_t>(sm.hist.cnt[b]);
+      hist_tile_task(seg, task.tile, io, sm.hist.cnt);
       __threadfence();
       __syncthreads();
       if (t == 0) {
@@ -227,124 +383,102 @@ __global__ void __launch_bounds__(kThreads, 3)
       __syncthreads();
       if (s_flag) {  // last HIST tile of the segment: scan the histogram
         __threadfence();
-        block_exclusive_scan_inplace(his, static_cast<int64_t>(seg.buckets) * seg.tiles,
-                                     sm.hist.wsum);
+        block_exclusive_scan_inplace(reinterpret_cast<int32_t *>(io.state + seg.state),
+                                     static_cast<int64_t>(seg.buckets) * seg.tiles, sm.hist.wsum);
         __threadfence();
         __syncthreads();
         if (t == 0) st_release_u32(&ctrl[task.seg].ready, 1u);
       }
     } else {
-      // ---- stable key/value scatter of a split tile ----
       if (t == 0) {
         bool ok = ld_acquire_u32(&ctrl[task.seg].ready) != 0u;
         if (!ok) {
           const uint64_t t0 = globaltimer_ns();
           while (!(ok = ld_acquire_u32(&ctrl[task.seg].ready) != 0u)) {
-            if (globaltimer_ns() - t0 > timeout_ns || fault_raised(abort_flag)) break;
+            if (globaltimer_ns() - t0 > io.timeout_ns || fault_raised(io.abort_flag)) break;
             __nanosleep(100);
           }
         }
         if (!ok) {
-          raise_fault(fault, EDPP_FAULT_TIMEOUT);
-          atomicOr(abort_flag, 1u);
+          raise_fault(io.fault, EDPP_FAULT_TIMEOUT);
+          atomicOr(io.abort_flag, 1u);
         }
         s_flag = ok ? 1 : 0;
         take_next();
       }
       __syncthreads();
-      if (s_flag) {
-        const unsigned mask = static_cast<unsigned>(seg.buckets - 1);
-        const int B = seg.buckets;
-        const int32_t *his = reinterpret_cast<const int32_t *>(state + seg.state);
-        for (int i = t; i < count; i += kThreads) {
-          sm.split.keys[i] = in0[gbase + i];
-          sm.split.vals[i] = in1[gbase + i];
-        }
-        for (int i = t; i < kWarps * B; i += kThreads) sm.split.cnt16[i] = 0;
-        __syncthreads();
-        uint16_t *my = sm.split.cnt16 + w * B;
-        const int kbits = 31 - __clz(B);
-        int32_t kk[kIters], vv[kIters];
-        uint32_t rk[kIters / 2];
-#pragma unroll
-        for (int it = 0; it < kIters; ++it) {
-          const int pos = w * kSeg + it * 32 + lane;
-          const bool valid = pos < count;
-          const int32_t key = valid ? sm.split.keys[pos] : 0;
-          const int32_t val = valid ? sm.split.vals[pos] : 0;
-          const int b = valid ? static_cast<int>(static_cast<unsigned>(key) & mask) : -1;
-          const unsigned vmask = __ballot_sync(0xffffffffu, valid);
-          unsigned peers;
-          if (kbits <= 5) {
-            peers = match_low_bits(static_cast<unsigned>(b), kbits, vmask);
-          } else {  // one leader lane per bucket, 5 votes on its lane number
-            if (valid) sm.split.last[w * B + b] = static_cast<uint8_t>(lane);
-            __syncwarp();
-            peers = match_low_bits(valid ? sm.split.last[w * B + b] : 0u, 5, vmask);
-          }
-          const unsigned lower = peers & lt;
-          const uint16_t before = valid ? my[b] : 0;
-          __syncwarp();
-          if (valid && lower == 0u) my[b] = static_cast<uint16_t>(before + __popc(peers));
-          __syncwarp();
-          kk[it] = key;
-          vv[it] = val;
-          const uint32_t r = static_cast<uint32_t>(before + __popc(lower));
-          if (it & 1) rk[it >> 1] |= r << 16;
-          else rk[it >> 1] = r;
-        }
-        __syncthreads();
-        // per bucket: exclusive prefix over warps; tile counts; tile offsets
-        if (t < 32) {
-          int32_t run_total = 0;
-          for (int b0 = 0; b0 < B; b0 += 32) {
-            const int b = b0 + lane;
-            int32_t tot = 0;
-            if (b < B) {
-              for (int ww = 0; ww < kWarps; ++ww) {
-                const int32_t c = sm.split.cnt16[ww * B + b];
-                sm.split.cnt16[ww * B + b] = static_cast<uint16_t>(tot);
-                tot += c;
-              }
-            }
-            int32_t incl = tot;
-#pragma unroll
-            for (int d = 1; d < 32; d <<= 1) {
-              const int32_t y = __shfl_up_sync(0xffffffffu, incl, d);
-              if (lane >= d) incl += y;
-            }
-            if (b < B) {
-              const int32_t off = run_total + incl - tot;
-              sm.split.toff[b] = off;
-              sm.split.gofs[b] = __ldcg(his + static_cast<int64_t>(b) * seg.tiles + task.tile) - off;
-            }
-            run_total += __shfl_sync(0xffffffffu, incl, 31);
-          }
-        }
-        __syncthreads();
-#pragma unroll
-        for (int it = 0; it < kIters; ++it) {
-          const int pos = w * kSeg + it * 32 + lane;
-          if (pos < count) {
-            const int b = static_cast<int>(static_cast<unsigned>(kk[it]) & mask);
-            const int r = static_cast<int>((rk[it >> 1] >> ((it & 1) * 16)) & 0xffffu);
-            const int s = sm.split.toff[b] + sm.split.cnt16[w * B + b] + r;
-            sm.split.keys[s] = kk[it];
-            sm.split.vals[s] = vv[it];
-          }
-        }
-        __syncthreads();
-        for (int s = t; s < count; s += kThreads) {
-          const int32_t key = sm.split.keys[s];
-          const int b = static_cast<int>(static_cast<unsigned>(key) & mask);
-          const int64_t o = seg.off + sm.split.gofs[b] + s;
-          out0[o] = key;
-          out1[o] = sm.split.vals[s];
-        }
-      }
+      if (s_flag) split_tile_task(seg, task.tile, io, sm);
     }
     __syncthreads();  // shared memory and s_task reused by the next task
   }
+}
+
+// ---- KINDS schedule: one launch per tile kind, one block per tile ----
+// Stream order separates the kinds, so no task waits on a flag; scan tiles
+// wait only on lower tiles of their own segment (lower block indices).
+
+__global__ void __launch_bounds__(kThreads, 6)
+    kind_scan_kernel(const DevSeg *__restrict__ segs, const DevTask *__restrict__ tasks, TaskIO io) {
+  __shared__ alignas(128) int32_t tile[kTile];
+  __shared__ TS32::Shared sh;
+  __shared__ alignas(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  const DevTask task = tasks[blockIdx.x];
+  DevSeg seg;
+  if (!task_in_plan(task, segs, io, seg)) {
+    if (threadIdx.x == 0) atomicOr(io.abort_flag, 1u);  // releases waiting tiles
+    return;
+  }
+  uint32_t phase = 0;
+  scan_tile_task(seg, task.tile, io, tile, sh, &bar, phase, [] {});
+}
+
+__global__ void __launch_bounds__(kThreads, 8)
+    kind_gather_kernel(const DevSeg *__restrict__ segs, const DevTask *__restrict__ tasks,
+                       TaskIO io) {
+  const DevTask task = tasks[blockIdx.x];
+  DevSeg seg;
+  if (task_in_plan(task, segs, io, seg)) gather_tile_task(seg, task.tile, io);
+}
+
+__global__ void __launch_bounds__(kThreads, 8)
+    kind_hist_kernel(const DevSeg *__restrict__ segs, const DevTask *__restrict__ tasks, TaskIO io) {
+  __shared__ uint32_t cnt[kMaxB];
+  const DevTask task = tasks[blockIdx.x];
+  DevSeg seg;
+  if (task_in_plan(task, segs, io, seg)) hist_tile_task(seg, task.tile, io, cnt);
+}
+
+// One block per split segment: exclusive scan of its histogram in place.
+__global__ void __launch_bounds__(kThreads)
+    kind_his_scan_kernel(const DevSeg *__restrict__ segs, const int32_t *__restrict__ split_segs,
+                         TaskIO io) {
+  __shared__ int32_t wsum[32];
+  const int i = split_segs[blockIdx.x];
+  if (i < 0 || i >= io.num_segs) {
+    if (threadIdx.x == 0) raise_fault(io.fault, EDPP_FAULT_PLAN);
+    return;
+  }
+  const DevSeg seg = segs[i];
+  if (seg.op != EDPP_BATCH_SPLIT) {
+    if (threadIdx.x == 0) raise_fault(io.fault, EDPP_FAULT_PLAN);
+    return;
+  }
+  block_exclusive_scan_inplace(reinterpret_cast<int32_t *>(io.state + seg.state),
+                               static_cast<int64_t>(seg.buckets) * seg.tiles, wsum);
+}
+
+__global__ void __launch_bounds__(kThreads, 3)
+    kind_split_kernel(const DevSeg *__restrict__ segs, const DevTask *__restrict__ tasks,
+                      TaskIO io) {
+  __shared__ BatchSmem sm;
+  const DevTask task = tasks[blockIdx.x];
+  DevSeg seg;
+  if (task_in_plan(task, segs, io, seg)) split_tile_task(seg, task.tile, io, sm);
 }
 
 }  // namespace
@@ -362,6 +496,9 @@ int build_plan(const edpp_segment *in, int num, const edpp_batch_tuning *tune, B
   const int defer = tune ? std::max(0, tune->split_defer_segments) : 1;
   const bool largest_first = tune ? tune->largest_first != 0 : true;
   p.blocks_per_sm = tune && tune->blocks_per_sm > 0 ? tune->blocks_per_sm : 4;
+  p.schedule = tune ? tune->schedule : EDPP_BATCH_SCHEDULE_KINDS;
+  if (p.schedule != EDPP_BATCH_SCHEDULE_KINDS && p.schedule != EDPP_BATCH_SCHEDULE_QUEUE)
+    return EDPP_EINVAL;
   if (largest_first)
     std::stable_sort(order.begin(), order.end(),
                      [&](int a, int b) { return in[a].length > in[b].length; });
@@ -431,11 +568,35 @@ int build_plan(const edpp_segment *in, int num, const edpp_batch_tuning *tune, B
     }
   }
   flush_due(true);
+  p.queue_tasks = static_cast<int64_t>(p.tasks.size());
+  if (p.schedule == EDPP_BATCH_SCHEDULE_KINDS) {
+    // per kind, segments in the given order, tiles ascending
+    std::vector<DevTask> scan, gather, split;
+    for (int i = 0; i < num; ++i) {
+      const DevSeg &d = p.segs[static_cast<size_t>(i)];
+      if (d.len == 0) continue;
+      auto &dst = d.op == EDPP_BATCH_SCAN ? scan : d.op == EDPP_BATCH_GATHER ? gather : split;
+      const int32_t kind = d.op == EDPP_BATCH_SCAN     ? kTaskScan
+                           : d.op == EDPP_BATCH_GATHER ? kTaskGather
+                                                       : kTaskSplit;
+      for (int t = 0; t < d.tiles; ++t) dst.push_back({i, t, kind, 0});
+      if (d.op == EDPP_BATCH_SPLIT) p.split_segs.push_back(i);
+    }
+    p.n_scan = static_cast<int64_t>(scan.size());
+    p.n_gather = static_cast<int64_t>(gather.size());
+    p.n_split = static_cast<int64_t>(split.size());
+    p.tasks = std::move(scan);
+    p.tasks.insert(p.tasks.end(), gather.begin(), gather.end());
+    p.tasks.insert(p.tasks.end(), split.begin(), split.end());
+  }
+  // the same layout for both schedules: the task area fits the queue form
   size_t o = kHdrB;
   p.off_segs = o;
   o += round_up(sizeof(DevSeg) * p.segs.size(), 256);
   p.off_tasks = o;
-  o += round_up(sizeof(DevTask) * p.tasks.size(), 256);
+  o += round_up(sizeof(DevTask) * static_cast<size_t>(p.queue_tasks), 256);
+  p.off_split_segs = o;
+  o += round_up(sizeof(int32_t) * p.segs.size(), 256);
   p.off_ctrl = o;
   o += round_up(sizeof(Ctrl) * p.segs.size(), 256);
   p.off_state = o;
@@ -472,7 +633,7 @@ size_t edpp_batch_plan_workspace_size(const edpp_batch_plan *plan) {
 }
 
 int edpp_batch_plan_num_tasks(const edpp_batch_plan *plan) {
-  return plan ? static_cast<int>(plan->impl.tasks.size()) : 0;
+  return plan ? static_cast<int>(plan->impl.queue_tasks) : 0;
 }
 
 int edpp_batch_plan_upload(const edpp_batch_plan *plan, void *ws, size_t ws_bytes, void *stream) {
@@ -488,6 +649,11 @@ int edpp_batch_plan_upload(const edpp_batch_plan *plan, void *ws, size_t ws_byte
   if (!p.tasks.empty() &&
       cudaMemcpyAsync(w + p.off_tasks, p.tasks.data(), sizeof(edpp::DevTask) * p.tasks.size(),
                       cudaMemcpyHostToDevice, st) != cudaSuccess)
+    return EDPP_ECUDA;
+  if (!p.split_segs.empty() &&
+      cudaMemcpyAsync(w + p.off_split_segs, p.split_segs.data(),
+                      sizeof(int32_t) * p.split_segs.size(), cudaMemcpyHostToDevice,
+                      st) != cudaSuccess)
     return EDPP_ECUDA;
   // pageable sources: make the copies complete before the plan can change
   return edpp::cuda_status(cudaStreamSynchronize(st));
@@ -510,6 +676,27 @@ int edpp_batch_launch(const edpp_batch_plan *plan, const int32_t *in0, const int
   if (cudaMemsetAsync(w + p.off_ctrl, 0, p.off_state - p.off_ctrl + p.scan_state_bytes, st) !=
       cudaSuccess)
     return EDPP_ECUDA;
+  const DevSeg *dsegs = reinterpret_cast<const DevSeg *>(w + p.off_segs);
+  const DevTask *dtasks = reinterpret_cast<const DevTask *>(w + p.off_tasks);
+  const TaskIO io{in0, in1, out0, out1, w + p.off_state, kDefaultWaitNs, fault,
+                  reinterpret_cast<unsigned *>(w + 8), aligned16(in0), p.num_segs};
+  if (p.schedule == EDPP_BATCH_SCHEDULE_KINDS) {
+    if (p.n_scan)
+      kind_scan_kernel<<<static_cast<unsigned>(p.n_scan), kThreads, 0, st>>>(dsegs, dtasks, io);
+    if (p.n_gather)
+      kind_gather_kernel<<<static_cast<unsigned>(p.n_gather), kThreads, 0, st>>>(
+          dsegs, dtasks + p.n_scan, io);
+    if (p.n_split) {
+      const DevTask *split_tasks = dtasks + p.n_scan + p.n_gather;
+      kind_hist_kernel<<<static_cast<unsigned>(p.n_split), kThreads, 0, st>>>(dsegs, split_tasks,
+                                                                              io);
+      kind_his_scan_kernel<<<static_cast<unsigned>(p.split_segs.size()), kThreads, 0, st>>>(
+          dsegs, reinterpret_cast<const int32_t *>(w + p.off_split_segs), io);
+      kind_split_kernel<<<static_cast<unsigned>(p.n_split), kThreads, 0, st>>>(dsegs, split_tasks,
+                                                                               io);
+    }
+    return launch_status();
+  }
   static std::once_flag occ_once[64];
   static cudaError_t occ_err[64];
   static int resident[64];
@@ -526,11 +713,8 @@ int edpp_batch_launch(const edpp_batch_plan *plan, const int32_t *in0, const int
   int64_t blocks = static_cast<int64_t>(device_sm_count()) * per_sm;
   blocks = min64(blocks, static_cast<int64_t>(p.tasks.size()));
   batch_kernel<<<static_cast<unsigned>(max64(blocks, 1)), kThreads, 0, st>>>(
-      reinterpret_cast<const DevSeg *>(w + p.off_segs),
-      reinterpret_cast<const DevTask *>(w + p.off_tasks), static_cast<int>(p.tasks.size()), in0,
-      in1, out0, out1, w + p.off_state, reinterpret_cast<Ctrl *>(w + p.off_ctrl),
-      reinterpret_cast<unsigned long long *>(w), reinterpret_cast<unsigned *>(w + 8),
-      aligned16(in0), kDefaultWaitNs, fault);
+      dsegs, dtasks, static_cast<int>(p.tasks.size()), io,
+      reinterpret_cast<Ctrl *>(w + p.off_ctrl), reinterpret_cast<unsigned long long *>(w));
   return launch_status();
 }
 
@@ -578,9 +762,10 @@ extern "C" int edpp_batch_run_plain(const edpp_segment *segs, int num_segs, cons
 // ---- autotuner ----------------------------------------------------------------------
 // Times every candidate schedule on this GPU for the given segments (CUDA
 // events around `reps` launches after one warm-up) and returns the fastest.
-// Candidates: blocks per SM {2,3,4,6,8} x split deferral {0,1,2,4} x
-// segment order {given, largest first}.  The workspace must fit the plan
-// (edpp_batch_plan_workspace_size; it does not depend on the tuning).
+// Candidates: the KINDS schedule, and the QUEUE schedule with blocks per SM
+// {1,2,3,4} x split deferral {0,1,2,4} x segment order {given, largest
+// first}.  The workspace must fit the plan (edpp_batch_plan_workspace_size;
+// it does not depend on the tuning).
 extern "C" int edpp_batch_autotune(const edpp_segment *segs, int num_segs, const int32_t *in0,
                                    const int32_t *in1, int32_t *out0, int32_t *out1, void *ws,
                                    size_t ws_bytes, void *stream, int reps,
@@ -595,34 +780,31 @@ extern "C" int edpp_batch_autotune(const edpp_segment *segs, int num_segs, const
   }
   float best_t = 1e30f;
   int status = EDPP_OK;
-  for (int bps : {1, 2, 3, 4}) {  // the launch clamps to the resident count
-    for (int defer : {0, 1, 2, 4}) {
-      for (int lf : {0, 1}) {
-        edpp_batch_tuning tu{bps, defer, lf, 0};
-        edpp_batch_plan *plan = nullptr;
-        status = edpp_batch_plan_create(segs, num_segs, &tu, &plan);
-        if (status != EDPP_OK) break;
-        status = edpp_batch_plan_upload(plan, ws, ws_bytes, stream);
-        if (status == EDPP_OK)
-          status = edpp_batch_launch(plan, in0, in1, out0, out1, ws, ws_bytes, stream);
-        if (status == EDPP_OK && cudaEventRecord(a, st) != cudaSuccess) status = EDPP_ECUDA;
-        for (int r = 0; r < reps && status == EDPP_OK; ++r)
-          status = edpp_batch_launch(plan, in0, in1, out0, out1, ws, ws_bytes, stream);
-        if (status == EDPP_OK && cudaEventRecord(b, st) != cudaSuccess) status = EDPP_ECUDA;
-        if (status == EDPP_OK) status = edpp_sync_status(stream, 0);
-        float ms = 0;
-        if (status == EDPP_OK && cudaEventElapsedTime(&ms, a, b) != cudaSuccess) status = EDPP_ECUDA;
-        edpp_batch_plan_destroy(plan);
-        if (status != EDPP_OK) break;
-        ms /= reps;
-        if (ms < best_t) {
-          best_t = ms;
-          *best = tu;
-        }
-      }
-      if (status != EDPP_OK) break;
-    }
+  std::vector<edpp_batch_tuning> cands{{0, 0, 0, EDPP_BATCH_SCHEDULE_KINDS}};
+  for (int bps : {1, 2, 3, 4})  // the launch clamps to the resident count
+    for (int defer : {0, 1, 2, 4})
+      for (int lf : {0, 1}) cands.push_back({bps, defer, lf, EDPP_BATCH_SCHEDULE_QUEUE});
+  for (const edpp_batch_tuning &tu : cands) {
+    edpp_batch_plan *plan = nullptr;
+    status = edpp_batch_plan_create(segs, num_segs, &tu, &plan);
     if (status != EDPP_OK) break;
+    status = edpp_batch_plan_upload(plan, ws, ws_bytes, stream);
+    if (status == EDPP_OK)
+      status = edpp_batch_launch(plan, in0, in1, out0, out1, ws, ws_bytes, stream);
+    if (status == EDPP_OK && cudaEventRecord(a, st) != cudaSuccess) status = EDPP_ECUDA;
+    for (int r = 0; r < reps && status == EDPP_OK; ++r)
+      status = edpp_batch_launch(plan, in0, in1, out0, out1, ws, ws_bytes, stream);
+    if (status == EDPP_OK && cudaEventRecord(b, st) != cudaSuccess) status = EDPP_ECUDA;
+    if (status == EDPP_OK) status = edpp_sync_status(stream, 0);
+    float ms = 0;
+    if (status == EDPP_OK && cudaEventElapsedTime(&ms, a, b) != cudaSuccess) status = EDPP_ECUDA;
+    edpp_batch_plan_destroy(plan);
+    if (status != EDPP_OK) break;
+    ms /= reps;
+    if (ms < best_t) {
+      best_t = ms;
+      *best = tu;
+    }
   }
   cudaEventDestroy(a);
   cudaEventDestroy(b);

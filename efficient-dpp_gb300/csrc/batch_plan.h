@@ -37,12 +37,18 @@ struct Ctrl {
 
 struct BatchPlanImpl {
   std::vector<DevSeg> segs;
+  // QUEUE schedule: the work queue in order.  KINDS schedule: scan tiles,
+  // then gather tiles, then split tiles (one entry per split tile).
   std::vector<DevTask> tasks;
+  std::vector<int32_t> split_segs;  // KINDS: segments whose histogram is scanned
+  int64_t n_scan = 0, n_gather = 0, n_split = 0;  // KINDS: tiles of each kind
+  int64_t queue_tasks = 0;  // tasks of the QUEUE form (a split tile counts twice)
   size_t scan_state_bytes = 0;  // zeroed per launch
   size_t state_bytes = 0;
-  size_t off_segs = 0, off_tasks = 0, off_ctrl = 0, off_state = 0, bytes = 0;
+  size_t off_segs = 0, off_tasks = 0, off_split_segs = 0, off_ctrl = 0, off_state = 0, bytes = 0;
   int num_segs = 0;
   int blocks_per_sm = 4;
+  int schedule = 0;  // edpp_batch_schedule
   int64_t total_elems = 0;
 };
 

@@ -190,17 +190,24 @@ int launch_batch(edpp_server *s, int k) {
   sl.plan.reset(plan);
   const edpp::BatchPlanImpl &p = plan->impl;
   if (p.bytes > sl.ws_bytes) return EDPP_ENOMEM;
+  // the plan's tables (segments, tasks, split segment list), as
+  // edpp_batch_plan_upload places them, through pinned staging
   const size_t seg_b = sizeof(edpp::DevSeg) * p.segs.size();
   const size_t task_b = sizeof(edpp::DevTask) * p.tasks.size();
-  if (seg_b + task_b > sl.staging_bytes) return EDPP_ENOMEM;
+  const size_t split_b = sizeof(int32_t) * p.split_segs.size();
+  if (seg_b + task_b + split_b > sl.staging_bytes) return EDPP_ENOMEM;
   char *stg = static_cast<char *>(sl.staging);
   std::memcpy(stg, p.segs.data(), seg_b);
   std::memcpy(stg + seg_b, p.tasks.data(), task_b);
+  if (split_b) std::memcpy(stg + seg_b + task_b, p.split_segs.data(), split_b);
   char *w = static_cast<char *>(sl.ws);
   cudaStream_t str = sl.stream;
   if (cudaMemcpyAsync(w + p.off_segs, stg, seg_b, cudaMemcpyHostToDevice, str) != cudaSuccess ||
       cudaMemcpyAsync(w + p.off_tasks, stg + seg_b, task_b, cudaMemcpyHostToDevice, str) !=
           cudaSuccess)
+    return EDPP_ECUDA;
+  if (split_b && cudaMemcpyAsync(w + p.off_split_segs, stg + seg_b + task_b, split_b,
+                                 cudaMemcpyHostToDevice, str) != cudaSuccess)
     return EDPP_ECUDA;
   // inputs
   for (auto &r : sl.reqs) {
@@ -334,12 +341,13 @@ int edpp_server_create(const edpp_server_config *cfg, edpp_server **out) {
   // of the batch in split segments of the maximum bucket count, and one
   // segment per request).
   const int64_t max_tiles = s->cfg.max_batch_elements / edpp::kBatchTile + s->cfg.max_batch_requests;
-  const size_t ws_bytes = 256 + 64 * static_cast<size_t>(s->cfg.max_batch_requests) * 3 +
+  const size_t ws_bytes = 256 + 64 * static_cast<size_t>(s->cfg.max_batch_requests) * 4 +
                           sizeof(edpp::DevTask) * 2 * static_cast<size_t>(max_tiles) +
                           static_cast<size_t>(max_tiles) *
                               (8 + 4 * static_cast<size_t>(edpp::kBatchMaxBuckets)) +
                           256 * static_cast<size_t>(s->cfg.max_batch_requests) * 2 + (1 << 20);
-  const size_t staging = sizeof(edpp::DevSeg) * static_cast<size_t>(s->cfg.max_batch_requests) +
+  const size_t staging = (sizeof(edpp::DevSeg) + sizeof(int32_t)) *
+                             static_cast<size_t>(s->cfg.max_batch_requests) +
                          sizeof(edpp::DevTask) * 2 * static_cast<size_t>(max_tiles);
   const size_t staging_alloc = staging + 256;  // + the abort word
   s->slots.resize(static_cast<size_t>(cfg->slots));

@@ -100,6 +100,7 @@ int edpp_sync_status(void *stream, int clear) {
     e = cudaMemcpyToSymbol(edpp::g_fault_word, &zero, sizeof(zero));
     if (e != cudaSuccess) return EDPP_ECUDA;
   }
+  if (v & EDPP_FAULT_PLAN) return EDPP_EINVAL;
   return v ? EDPP_ETIMEOUT : EDPP_OK;
 }
 

@@ -30,19 +30,29 @@ ALIGN = 64  # segment offsets in elements (256 bytes)
 TUNING_TABLE = Path(__file__).resolve().parent.parent / "tuning" / "batch_gb300.json"
 
 
+SCHEDULE_KINDS, SCHEDULE_QUEUE = 0, 1
+SCHEDULE_NAMES = {SCHEDULE_KINDS: "kinds", SCHEDULE_QUEUE: "queue"}
+
+
 class Tuning(ctypes.Structure):
+    """edpp_batch_tuning: `schedule` KINDS (one launch per tile kind, the
+    default) or QUEUE (one persistent work-queue launch, which the other
+    three knobs tune)."""
     _fields_ = [("blocks_per_sm", ctypes.c_int32), ("split_defer_segments", ctypes.c_int32),
-                ("largest_first", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("largest_first", ctypes.c_int32), ("schedule", ctypes.c_int32)]
 
     def as_dict(self):
         return {"blocks_per_sm": self.blocks_per_sm,
                 "split_defer_segments": self.split_defer_segments,
-                "largest_first": self.largest_first}
+                "largest_first": self.largest_first,
+                "schedule": SCHEDULE_NAMES.get(self.schedule, str(self.schedule))}
 
     @classmethod
     def from_dict(cls, d):
+        sched = d.get("schedule", "kinds")
+        sched = {v: k for k, v in SCHEDULE_NAMES.items()}.get(sched, sched)
         return cls(int(d["blocks_per_sm"]), int(d["split_defer_segments"]),
-                   int(d["largest_first"]), 0)
+                   int(d["largest_first"]), int(sched))
 
 
 def _draw(seed: int, i: int) -> int:

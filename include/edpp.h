@@ -50,6 +50,8 @@ typedef enum {
 /* Bits of the device fault word (edpp_device_fault). */
 #define EDPP_FAULT_TIMEOUT 0x1u   /* look-back / dependency wait ran out    */
 #define EDPP_FAULT_TMA     0x2u   /* a TMA transaction wait ran out         */
+#define EDPP_FAULT_PLAN    0x4u   /* a batch task named a segment or tile
+                                     outside the uploaded plan's tables     */
 
 /* ---- enums mirroring the reference's types (opencl/types.h:8-47) -------- */
 
@@ -85,9 +87,10 @@ const char *edpp_status_string(int status);
 /* Library version, as major*10000 + minor*100 + patch. */
 int edpp_version(void);
 
-/* Wait for `stream`, then report the first error: a CUDA error, or
- * EDPP_ETIMEOUT if a kernel recorded a fault since the last clear.
- * clear != 0 resets the fault word afterwards. */
+/* Wait for `stream`, then report the first error: a CUDA error, or, if a
+ * kernel recorded a fault since the last clear, EDPP_EINVAL for
+ * EDPP_FAULT_PLAN and EDPP_ETIMEOUT otherwise.  clear != 0 resets the fault
+ * word afterwards. */
 int edpp_sync_status(void *stream, int clear);
 
 /* Read (and optionally clear) the device fault word of the current device.
@@ -359,14 +362,25 @@ typedef struct {
     int32_t reserved;
 } edpp_segment;
 
+/* How a batch runs on the GPU:
+ *   KINDS  one launch per kind of tile over every segment of that kind (scan
+ *          tiles; gather tiles; split histogram tiles, the per-segment
+ *          histogram scans, split scatter tiles), each sized for its kind
+ *   QUEUE  one persistent launch whose blocks take all tiles from one work
+ *          queue (blocks_per_sm, split_defer_segments, largest_first apply) */
+typedef enum {
+    EDPP_BATCH_SCHEDULE_KINDS = 0,
+    EDPP_BATCH_SCHEDULE_QUEUE = 1
+} edpp_batch_schedule;
+
 /* Scheduling knobs (chosen per size class by the project's autotuner,
  * edpp_batch_autotune).  Zero-initialised = defaults. */
 typedef struct {
-    int32_t blocks_per_sm;         /* persistent grid: blocks per SM (default 4)  */
-    int32_t split_defer_segments;  /* SPLIT tiles queued this many segments after
-                                      their HIST tiles (default 1)               */
-    int32_t largest_first;         /* 1: queue segments by descending length      */
-    int32_t reserved;
+    int32_t blocks_per_sm;         /* QUEUE: blocks per SM (default 4)            */
+    int32_t split_defer_segments;  /* QUEUE: SPLIT tiles queued this many segments
+                                      after their HIST tiles (default 1)         */
+    int32_t largest_first;         /* QUEUE: segments by descending length        */
+    int32_t schedule;              /* edpp_batch_schedule (default KINDS)         */
 } edpp_batch_tuning;
 
 typedef struct edpp_batch_plan edpp_batch_plan;  /* opaque, host side */
@@ -376,13 +390,15 @@ int edpp_batch_plan_create(const edpp_segment *segs, int num_segs,
                            const edpp_batch_tuning *tuning, edpp_batch_plan **plan);
 void edpp_batch_plan_destroy(edpp_batch_plan *plan);
 size_t edpp_batch_plan_workspace_size(const edpp_batch_plan *plan);
+/* Tile tasks of the batch (a split tile counts twice: histogram and scatter). */
 int edpp_batch_plan_num_tasks(const edpp_batch_plan *plan);
 /* Copy the plan's tables into the workspace (synchronises `stream`). */
 int edpp_batch_plan_upload(const edpp_batch_plan *plan, void *ws, size_t ws_bytes,
                            void *stream);
-/* Run every segment in one persistent launch (plus two memsets).  The
- * workspace must hold an uploaded plan.  Stream-ordered; may be captured in a
- * CUDA graph and replayed while the plan and arrays stay the same. */
+/* Run every segment: one launch per tile kind (KINDS) or one persistent
+ * launch (QUEUE), plus two memsets.  The workspace must hold an uploaded
+ * plan.  Stream-ordered; may be captured in a CUDA graph and replayed while
+ * the plan and arrays stay the same. */
 int edpp_batch_launch(const edpp_batch_plan *plan, const int32_t *in0,
                       const int32_t *in1, int32_t *out0, int32_t *out1, void *ws,
                       size_t ws_bytes, void *stream);

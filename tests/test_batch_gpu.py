@@ -1,6 +1,7 @@
-"""The batched persistent kernel against the oracle (bit-exact) and against
-the plain per-segment C-ABI calls, including the 4096-segment workload and
-CUDA-graph replay."""
+"""The batched form against the oracle (bit-exact) and against the plain
+per-segment C-ABI calls, including the 4096-segment workload and CUDA-graph
+replay, under both schedules: KINDS (one launch per tile kind) and QUEUE (one
+persistent work-queue launch)."""
 import numpy as np
 import pytest
 
@@ -43,13 +44,13 @@ def _mask_unused(segs, a0, a1):
 SIZES = [1, 2, 31, 4095, 4096, 4097, 8192, 12289, 100003, 1 << 18]
 
 
-@pytest.mark.parametrize("tuning", [None, (2, 0, 0), (8, 4, 1)])
+@pytest.mark.parametrize("tuning", [None, (0, 0, 0, 0), (2, 0, 0, 1), (8, 4, 1, 1)])
 def test_mixed_small_batch_vs_oracle(cuda, edpp, batch, tuning):
     sizes = SIZES * 3
     ops = [i % 3 for i in range(len(sizes))]
     segs = batch.layout(sizes, ops, buckets=64)
     in0, in1 = batch.gen_inputs(segs, seed=11)
-    tu = batch.Tuning(*tuning, 0) if tuning else None
+    tu = batch.Tuning(*tuning) if tuning else None
     o0, o1, _ = _run_batch(batch, cuda, segs, in0, in1, tu)
     assert edpp.sync_status() == edpp.EDPP_OK
     e0, e1 = reference_outputs(segs, in0, in1)
@@ -58,23 +59,25 @@ def test_mixed_small_batch_vs_oracle(cuda, edpp, batch, tuning):
     np.testing.assert_array_equal(g1, e1)
 
 
+@pytest.mark.parametrize("schedule", [0, 1])
 @pytest.mark.parametrize("buckets", [1, 2, 16, 64, 256])
-def test_split_bucket_counts(cuda, edpp, batch, buckets):
+def test_split_bucket_counts(cuda, edpp, batch, buckets, schedule):
     segs = batch.layout([70001, 4096, 9000], [1, 1, 1], buckets=buckets)
     in0, in1 = batch.gen_inputs(segs, seed=12)
-    o0, o1, _ = _run_batch(batch, cuda, segs, in0, in1)
+    o0, o1, _ = _run_batch(batch, cuda, segs, in0, in1, batch.Tuning(3, 1, 1, schedule))
     e0, e1 = reference_outputs(segs, in0, in1)
     g0, g1 = _mask_unused(segs, to_host(o0), to_host(o1))
     np.testing.assert_array_equal(g0, e0)
     np.testing.assert_array_equal(g1, e1)
 
 
-def test_unaligned_segment_offsets(cuda, edpp, batch):
+@pytest.mark.parametrize("schedule", [0, 1])
+def test_unaligned_segment_offsets(cuda, edpp, batch, schedule):
     # offsets that are not multiples of 4 elements: the bulk-copy path is off
     segs = batch.layout([5000, 7001, 9003], [0, 1, 2])
     segs["offset"] += np.array([1, 3, 2])
     in0, in1 = batch.gen_inputs(segs, seed=13)
-    o0, o1, _ = _run_batch(batch, cuda, segs, in0, in1)
+    o0, o1, _ = _run_batch(batch, cuda, segs, in0, in1, batch.Tuning(3, 1, 1, schedule))
     e0, e1 = reference_outputs(segs, in0, in1)
     g0, g1 = _mask_unused(segs, to_host(o0), to_host(o1))
     np.testing.assert_array_equal(g0, e0)
@@ -93,6 +96,11 @@ def test_config5_batch_equals_plain_and_graph_replay(cuda, edpp, batch):
     batch.run_plain(segs, d0, d1, p0, p1, pws)
     assert edpp.sync_status() == edpp.EDPP_OK
     assert cuda.equal(o0, p0) and cuda.equal(o1, p1)
+    # the work-queue schedule gives the same arrays
+    r0, r1, _ = _run_batch(batch, cuda, segs, in0, in1, batch.Tuning(3, 4, 1, 1))
+    assert edpp.sync_status() == edpp.EDPP_OK
+    assert cuda.equal(r0, p0) and cuda.equal(r1, p1)
+    del r0, r1
     # spot-check some segments of every op against the oracle
     pick = [i for op in (0, 1, 2) for i in np.nonzero(segs["op"] == op)[0][:3]]
     sub = segs[pick]

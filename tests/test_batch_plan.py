@@ -35,9 +35,21 @@ def test_plan_tasks_and_workspace(batch):
     expect = sum(t * (2 if op == 1 else 1) for t, op in zip(tiles, [0, 1, 2, 1, 0, 2]))
     assert plan.num_tasks == expect
     assert plan.workspace_bytes > 0
-    for tu in (batch.Tuning(2, 0, 0, 0), batch.Tuning(8, 4, 1, 0)):
+    for tu in (batch.Tuning(2, 0, 0, 0), batch.Tuning(8, 4, 1, 0), batch.Tuning(2, 0, 0, 1),
+               batch.Tuning(8, 4, 1, 1)):
         p2 = batch.Plan(segs, tu)
         assert p2.num_tasks == expect and p2.workspace_bytes == plan.workspace_bytes
+
+
+def test_plan_rejects_bad_schedule(batch, edpp):
+    segs = batch.layout([4096], [0])
+    h = ctypes.c_void_p()
+    tu = batch.Tuning(2, 0, 0, 7)
+    assert edpp.lib().edpp_batch_plan_create(ctypes.c_void_p(segs.ctypes.data), 1, ctypes.byref(tu),
+                                             ctypes.byref(h)) == edpp.EDPP_EINVAL
+    assert batch.Tuning.from_dict({"blocks_per_sm": 3, "split_defer_segments": 4,
+                                   "largest_first": 1}).schedule == batch.SCHEDULE_KINDS
+    assert batch.Tuning.from_dict(batch.Tuning(3, 4, 1, 1).as_dict()).schedule == batch.SCHEDULE_QUEUE
 
 
 def test_plan_rejects_bad_segments(batch, edpp):

@@ -69,17 +69,19 @@ def _run(srv, serve, reqs, concurrent):
     return outs, timings
 
 
-def test_alone_equals_mix_equals_oracle(cuda, edpp, serve):
+@pytest.mark.parametrize("schedule", [0, 1])  # batches as KINDS launches / one QUEUE launch
+def test_alone_equals_mix_equals_oracle(cuda, edpp, serve, schedule):
     sizes = [4096, 1, 777, 100003, 1 << 20, 3 << 18, 65536, 4097, 250000, 12345] * 4
     segs, in0, in1, reqs = _requests(edpp, serve, sizes, seed=21)
     e0, e1 = reference_outputs(segs, in0, in1)
-    with serve.Server(pool_bytes=256 << 20, slots=3) as srv:
+    tu = serve.Tuning(3, 1, 1, schedule)
+    with serve.Server(pool_bytes=256 << 20, slots=3, tuning=tu) as srv:
         alone, _ = _run(srv, serve, reqs, concurrent=False)
         mix3, _ = _run(srv, serve, reqs, concurrent=True)
         assert srv.stats()["completed"] == 2 * len(reqs)
     # one slot: requests arriving while a batch runs queue up and are
     # admitted together into the next batch
-    with serve.Server(pool_bytes=256 << 20, slots=1) as srv:
+    with serve.Server(pool_bytes=256 << 20, slots=1, tuning=tu) as srv:
         mix, lat = _run(srv, serve, reqs, concurrent=True)
         stats = srv.stats()
     for i in range(len(reqs)):
