@@ -1,26 +1,31 @@
 // batch.cu — many uneven segments of scan / stable split / permutation gather
-// in one persistent, work-queue-scheduled launch.
+// from one uploaded plan, in a handful of launches.
 //
-// The host planner (below) turns a segment table into a task queue.  Every
-// task is one tile of one segment:
+// The host planner (below) cuts every segment into tiles of kTile elements.
+// Tile kinds:
 //   SCAN     exclusive int32 scan tile; tiles of a segment are chained by a
 //            decoupled look-back over the segment's own tile states
 //   GATHER   out0[i] = in0[in1[i]] for a tile, indices local to the segment
 //   HIST     bucket counts of a split tile -> column t of the segment's
-//            bucket-major histogram his[b*T + t]; the block that finishes a
-//            segment's last HIST tile scans that histogram in place and
-//            publishes the segment's ready flag (release)
-//   SPLIT    stable key/value scatter of a tile once the ready flag is set
-//            (acquire); same ranking as split.cu, 64-bucket-class tiles
-// Blocks take tasks from one atomic ticket in queue order.  A task waits only
-// on tasks earlier in the queue (look-back predecessors, its segment's HIST
-// tiles), which running blocks already hold, so the schedule always makes
-// progress; every wait is bounded by %globaltimer and reports
-// EDPP_FAULT_TIMEOUT instead of hanging.
+//            bucket-major histogram his[b*T + t]
+//   SPLIT    stable key/value scatter of a tile once the segment's histogram
+//            is scanned; same ranking as split.cu, 64-bucket-class tiles
 //
-// Tuning (edpp_batch_tuning, chosen per size class by edpp_batch_autotune):
-// blocks per SM of the persistent grid, how many segments a split's SPLIT
-// tasks are deferred behind its HIST tasks, and the segment order.
+// Two schedules (edpp_batch_tuning.schedule):
+//   KINDS  one launch per kind, one block per tile: scan tiles, gather tiles,
+//          HIST tiles, one block per split segment scanning its histogram,
+//          SPLIT tiles.  Stream order separates the kinds; a scan tile waits
+//          only on lower tiles of its segment (lower block indices).
+//   QUEUE  one persistent kernel; blocks take tasks from one atomic ticket in
+//          queue order.  The block that finishes a segment's last HIST tile
+//          scans the histogram and publishes a ready flag (release) that the
+//          SPLIT tiles acquire.  A task waits only on tasks earlier in the
+//          queue, which running blocks already hold, so the schedule always
+//          makes progress.  Knobs (chosen per size class by
+//          edpp_batch_autotune): blocks per SM, how many segments a split's
+//          SPLIT tasks trail its HIST tasks, and the segment order.
+// Every wait is bounded by %globaltimer and reports EDPP_FAULT_TIMEOUT
+// instead of hanging.
 #include <algorithm>
 #include <cstring>
 #include <mutex>

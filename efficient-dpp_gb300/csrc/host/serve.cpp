@@ -8,7 +8,7 @@
 //   2. admits waiting requests in arrival order while device memory in the
 //      pool and a batch slot (stream) are free — admission by free HBM;
 //   3. packs the admitted requests into one batch: copies their inputs into
-//      pool-resident buffers, plans and launches one persistent batch kernel,
+//      pool-resident buffers, plans and launches the batch kernels,
 //      and copies the outputs back, all stream-ordered on the slot's stream.
 // Up to `slots` batches are in flight at once on separate streams, so
 // requests that arrive while others run are admitted as memory and slots

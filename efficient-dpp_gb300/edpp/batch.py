@@ -4,7 +4,7 @@
     in0, in1 = gen_inputs(segs, seed=4)          # numpy, seeded
     plan = Plan(segs, tuning)                    # host planner (C++)
     ws = plan.workspace(device); plan.upload(ws)
-    plan.launch(d_in0, d_in1, d_out0, d_out1, ws)   # one persistent launch
+    plan.launch(d_in0, d_in1, d_out0, d_out1, ws)   # one launch per tile kind
     run_plain(segs, ...)                         # one C-ABI call per segment
 
 Segment table rows follow edpp_segment: offset, length, op, buckets.

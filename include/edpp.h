@@ -338,7 +338,7 @@ int edpp_scan_exclusive_i32_noalloc(const int32_t *in, int32_t *out, int64_t len
                                     void *stream);
 int64_t edpp_scan_exclusive_i32_noalloc_max_length(void);
 
-/* ---- batched segments (one persistent launch) --------------------------- */
+/* ---- batched segments (one plan, a handful of launches) ----------------- */
 
 /* Operations a batch segment can run.  Results equal the plain calls:
  *   SCAN    out0 = exclusive int32 scan of in0            (edpp_scan_exclusive_i32)
@@ -458,7 +458,7 @@ typedef struct edpp_server edpp_server;  /* opaque */
  * arenas of pool_bytes/4), per-slot streams and workspaces, and a scheduler
  * thread.  One scheduler loop retires finished batches, admits waiting
  * requests in arrival order while pool memory and a slot are free, and
- * launches each batch as one persistent kernel between its copies.  No
+ * launches each batch (config->tuning's schedule) between its copies.  No
  * reference counterpart. */
 int edpp_server_create(const edpp_server_config *cfg, edpp_server **server);
 /* Thread-safe, non-blocking.  EDPP_EINVAL for a malformed request or one
