@@ -76,39 +76,60 @@ union __align__(128) BatchSmem {
   } hist;
 };
 
-// Exclusive scan of p[0..m) in place by the whole block (m up to millions).
+// Exclusive scan of p[0..m) in place by the whole block (m up to millions),
+// in rounds of kThreads x 4 consecutive elements (p 16-byte aligned: one
+// vector per thread), carrying the running total between rounds.
 __device__ void block_exclusive_scan_inplace(int32_t *p, int64_t m, int32_t *wsum) {
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-  const int64_t per = (m + kThreads - 1) / kThreads;
-  const int64_t lo = min64(m, t * per), hi = min64(m, lo + per);
-  uint32_t s = 0;
-  for (int64_t i = lo; i < hi; ++i) s += static_cast<uint32_t>(__ldcg(p + i));
-  uint32_t incl = s;
+  constexpr int kRound = kThreads * 4;
+  uint32_t carry = 0;
+  for (int64_t base = 0; base < m; base += kRound) {
+    const int64_t i0 = base + 4 * t;
+    uint32_t v[4] = {0u, 0u, 0u, 0u};
+    if (i0 + 3 < m) {
+      const int4 q = __ldcg(reinterpret_cast<const int4 *>(p + i0));
+      v[0] = static_cast<uint32_t>(q.x), v[1] = static_cast<uint32_t>(q.y);
+      v[2] = static_cast<uint32_t>(q.z), v[3] = static_cast<uint32_t>(q.w);
+    } else {
 #pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
-    if (lane >= d) incl += y;
-  }
-  if (lane == 31) wsum[w] = static_cast<int32_t>(incl);
-  __syncthreads();
-  if (w == 0) {
-    const uint32_t x = lane < kWarps ? static_cast<uint32_t>(wsum[lane]) : 0u;
-    uint32_t xi = x;
+      for (int k = 0; k < 4; ++k)
+        if (i0 + k < m) v[k] = static_cast<uint32_t>(__ldcg(p + i0 + k));
+    }
+    const uint32_t s = v[0] + v[1] + v[2] + v[3];
+    uint32_t incl = s;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, xi, d);
-      if (lane >= d) xi += y;
+      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= d) incl += y;
     }
-    if (lane < kWarps) wsum[lane] = static_cast<int32_t>(xi - x);
+    if (lane == 31) wsum[w] = static_cast<int32_t>(incl);
+    __syncthreads();
+    uint32_t wpre = 0, total = 0;
+#pragma unroll
+    for (int k = 0; k < kWarps; ++k) {
+      const uint32_t x = static_cast<uint32_t>(wsum[k]);
+      if (k < w) wpre += x;
+      total += x;
+    }
+    uint32_t run = carry + wpre + (incl - s);
+    if (i0 + 3 < m) {
+      int4 q;
+      q.x = static_cast<int32_t>(run);
+      q.y = static_cast<int32_t>(run += v[0]);
+      q.z = static_cast<int32_t>(run += v[1]);
+      q.w = static_cast<int32_t>(run += v[2]);
+      *reinterpret_cast<int4 *>(p + i0) = q;
+    } else {
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (i0 + k < m) {
+          p[i0 + k] = static_cast<int32_t>(run);
+          run += v[k];
+        }
+    }
+    carry += total;
+    __syncthreads();  // wsum is rewritten by the next round
   }
-  __syncthreads();
-  uint32_t run = static_cast<uint32_t>(wsum[w]) + (incl - s);
-  for (int64_t i = lo; i < hi; ++i) {
-    const uint32_t v = static_cast<uint32_t>(__ldcg(p + i));
-    p[i] = static_cast<int32_t>(run);
-    run += v;
-  }
-  __syncthreads();
 }
 
 // ---- tile task bodies, shared by the work-queue kernel and the per-kind kernels ----
@@ -119,7 +140,8 @@ struct TaskIO {
   char *state;
   uint64_t timeout_ns;
   unsigned *fault, *abort_flag;
-  bool tma;
+  bool tma;   // in0 16-byte aligned
+  bool tma1;  // in1 16-byte aligned
   int num_segs;
 };
 
@@ -217,12 +239,32 @@ __device__ __forceinline__ void hist_tile_task(const DevSeg &seg, int tile, cons
   const int count = static_cast<int>(min64(kTile, seg.len - tile_base));
   const int64_t gbase = seg.off + tile_base;
   const unsigned mask = static_cast<unsigned>(seg.buckets - 1);
+  // all of this thread's keys are loaded before the first count
+  int32_t k[kTile / kThreads];
+  const int32_t *src = io.in0 + gbase;
+  if (count == kTile && io.tma && (gbase & 3) == 0) {  // 16-byte aligned full tile
+#pragma unroll
+    for (int q = 0; q < kTile / kThreads / 4; ++q) {
+      const int4 v = __ldcs(reinterpret_cast<const int4 *>(src) + q * kThreads + t);
+      k[4 * q] = v.x, k[4 * q + 1] = v.y, k[4 * q + 2] = v.z, k[4 * q + 3] = v.w;
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < kTile / kThreads / 4; ++q)
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int i = 4 * (q * kThreads + t) + e;
+        k[4 * q + e] = i < count ? src[i] : 0;
+      }
+  }
   for (int b = t; b < seg.buckets; b += kThreads) cnt[b] = 0;
   __syncthreads();
-  for (int i0 = 0; i0 < kTile; i0 += kThreads) {
-    const int i = i0 + t;
-    if (i < count) atomicAdd(&cnt[static_cast<unsigned>(io.in0[gbase + i]) & mask], 1u);
-  }
+#pragma unroll
+  for (int q = 0; q < kTile / kThreads / 4; ++q)
+#pragma unroll
+    for (int e = 0; e < 4; ++e)
+      if (4 * (q * kThreads + t) + e < count)
+        atomicAdd(&cnt[static_cast<unsigned>(k[4 * q + e]) & mask], 1u);
   __syncthreads();
   int32_t *his = reinterpret_cast<int32_t *>(io.state + seg.state);
   for (int b = t; b < seg.buckets; b += kThreads)
@@ -231,9 +273,12 @@ __device__ __forceinline__ void hist_tile_task(const DevSeg &seg, int tile, cons
 
 // Stable key/value scatter of one split tile; the segment's histogram is
 // scanned (his[b*T + t] = first output index of bucket b from tile t).
-// Same ranking as split.cu.
+// Same ranking as split.cu.  The tile comes in by bulk copies (its
+// 16-byte-aligned part) on `bar`; warp 0 loads the tile's first 64 run
+// starts before the ranking, so that round trip overlaps it.
+constexpr int kHisPre = 2;  // run starts per lane of warp 0 loaded early
 __device__ __forceinline__ void split_tile_task(const DevSeg &seg, int tile, const TaskIO &io,
-                                                BatchSmem &sm) {
+                                                BatchSmem &sm, uint64_t *bar, uint32_t &phase) {
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
   const unsigned lt = lanemask_lt_b();
   const int64_t tile_base = static_cast<int64_t>(tile) * kTile;
@@ -242,11 +287,30 @@ __device__ __forceinline__ void split_tile_task(const DevSeg &seg, int tile, con
   const unsigned mask = static_cast<unsigned>(seg.buckets - 1);
   const int B = seg.buckets;
   const int32_t *his = reinterpret_cast<const int32_t *>(io.state + seg.state);
-  for (int i = t; i < count; i += kThreads) {
+  const uint32_t bulk =
+      (io.tma && io.tma1 && (gbase & 3) == 0) ? (static_cast<uint32_t>(count) * 4u) & ~15u : 0u;
+  if (t == 0 && bulk) {
+    mbar_arrive_expect_tx(bar, 2 * bulk);
+    tma_load_1d(sm.split.keys, io.in0 + gbase, bulk, bar);
+    tma_load_1d(sm.split.vals, io.in1 + gbase, bulk, bar);
+  }
+  for (int i = static_cast<int>(bulk / 4) + t; i < count; i += kThreads) {
     sm.split.keys[i] = io.in0[gbase + i];
     sm.split.vals[i] = io.in1[gbase + i];
   }
+  int32_t his_pre[kHisPre] = {0, 0};
+  if (w == 0) {
+#pragma unroll
+    for (int j = 0; j < kHisPre; ++j) {
+      const int b = j * 32 + lane;
+      if (b < B) his_pre[j] = __ldcg(his + static_cast<int64_t>(b) * seg.tiles + tile);
+    }
+  }
   for (int i = t; i < kWarps * B; i += kThreads) sm.split.cnt16[i] = 0;
+  if (bulk) {
+    if (!mbar_wait_bounded(bar, phase, io.timeout_ns, io.fault)) atomicOr(io.abort_flag, 1u);
+    phase ^= 1u;
+  }
   __syncthreads();
   uint16_t *my = sm.split.cnt16 + w * B;
   const int kbits = 31 - __clz(B);
@@ -302,7 +366,11 @@ __device__ __forceinline__ void split_tile_task(const DevSeg &seg, int tile, con
       if (b < B) {
         const int32_t off = run_total + incl - tot;
         sm.split.toff[b] = off;
-        sm.split.gofs[b] = __ldcg(his + static_cast<int64_t>(b) * seg.tiles + tile) - off;
+        const int j = b0 / 32;
+        const int32_t start = j == 0   ? his_pre[0]
+                              : j == 1 ? his_pre[1]
+                                       : __ldcg(his + static_cast<int64_t>(b) * seg.tiles + tile);
+        sm.split.gofs[b] = start - off;
       }
       run_total += __shfl_sync(0xffffffffu, incl, 31);
     }
@@ -412,9 +480,12 @@ __global__ void __launch_bounds__(kThreads, 3)
         take_next();
       }
       __syncthreads();
-      if (s_flag) split_tile_task(seg, task.tile, io, sm);
+      if (s_flag) split_tile_task(seg, task.tile, io, sm, &bar, phase);
     }
-    __syncthreads();  // shared memory and s_task reused by the next task
+    // this task's generic accesses of shared memory before the next task's
+    // bulk copies into it; shared memory and s_task reused by the next task
+    fence_proxy_async_smem();
+    __syncthreads();
   }
 }
 
@@ -481,9 +552,16 @@ __global__ void __launch_bounds__(kThreads, 3)
     kind_split_kernel(const DevSeg *__restrict__ segs, const DevTask *__restrict__ tasks,
                       TaskIO io) {
   __shared__ BatchSmem sm;
+  __shared__ alignas(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
   const DevTask task = tasks[blockIdx.x];
   DevSeg seg;
-  if (task_in_plan(task, segs, io, seg)) split_tile_task(seg, task.tile, io, sm);
+  uint32_t phase = 0;
+  if (task_in_plan(task, segs, io, seg)) split_tile_task(seg, task.tile, io, sm, &bar, phase);
 }
 
 }  // namespace
@@ -684,7 +762,8 @@ int edpp_batch_launch(const edpp_batch_plan *plan, const int32_t *in0, const int
   const DevSeg *dsegs = reinterpret_cast<const DevSeg *>(w + p.off_segs);
   const DevTask *dtasks = reinterpret_cast<const DevTask *>(w + p.off_tasks);
   const TaskIO io{in0, in1, out0, out1, w + p.off_state, kDefaultWaitNs, fault,
-                  reinterpret_cast<unsigned *>(w + 8), aligned16(in0), p.num_segs};
+                  reinterpret_cast<unsigned *>(w + 8), aligned16(in0), aligned16(in1),
+                  p.num_segs};
   if (p.schedule == EDPP_BATCH_SCHEDULE_KINDS) {
     if (p.n_scan)
       kind_scan_kernel<<<static_cast<unsigned>(p.n_scan), kThreads, 0, st>>>(dsegs, dtasks, io);
