@@ -165,10 +165,11 @@ __device__ __forceinline__ bool task_in_plan(const DevTask &task, const DevSeg *
 // Exclusive scan of one tile with a decoupled look-back over the segment's
 // own tile states.  `released()` runs (every thread) once no other task can
 // wait on this one any more: after the inclusive prefix is published.
-template <typename F>
+template <typename TS, int NT, int CHUNKS, typename F>
 __device__ __forceinline__ void scan_tile_task(const DevSeg &seg, int tile, const TaskIO &io,
-                                               int32_t *tile_smem, TS32::Shared &sh,
+                                               int32_t *tile_smem, typename TS::Shared &sh,
                                                uint64_t *bar, uint32_t &phase, F released) {
+  static_assert(TS::kTile == kTile, "batch tile size");
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
   const int64_t tile_base = static_cast<int64_t>(tile) * kTile;
   const int count = static_cast<int>(min64(kTile, seg.len - tile_base));
@@ -177,18 +178,18 @@ __device__ __forceinline__ void scan_tile_task(const DevSeg &seg, int tile, cons
   st.bind(io.state + seg.state, seg.tiles);
   const bool tma_ok = io.tma && ((gbase & 3) == 0);  // 16-byte aligned tile start
   const uint32_t bulk =
-      stage_tile<int32_t, kTile, kThreads>(tile_smem, io.in0 + gbase, count, tma_ok, bar);
+      stage_tile<int32_t, kTile, NT>(tile_smem, io.in0 + gbase, count, tma_ok, bar);
   if (bulk) {
     if (!mbar_wait_bounded(bar, phase, io.timeout_ns, io.fault)) atomicOr(io.abort_flag, 1u);
     phase ^= 1u;
   }
   __syncthreads();
-  Chunk<int32_t> c[kChunks];
-  int32_t wex[kChunks];
-  TS32::phase1(tile_smem, c, wex, sh);
+  Chunk<int32_t> c[CHUNKS];
+  int32_t wex[CHUNKS];
+  TS::phase1(tile_smem, c, wex, sh);
   __syncthreads();
   if (w == 0) {
-    const int32_t agg = TS32::phase2_warp0(sh, lane);
+    const int32_t agg = TS::phase2_warp0(sh, lane);
     int32_t prefix = 0;
     bool ok = true;
     if (tile == 0) {
@@ -201,8 +202,8 @@ __device__ __forceinline__ void scan_tile_task(const DevSeg &seg, int tile, cons
   }
   released();
   __syncthreads();
-  TS32::phase3<false>(c, wex, sh, sh.prefix);
-  TS32::store(io.out0, gbase, count, c, (reinterpret_cast<uintptr_t>(io.out0 + gbase) & 15) == 0);
+  TS::template phase3<false>(c, wex, sh, sh.prefix);
+  TS::store(io.out0, gbase, count, c, (reinterpret_cast<uintptr_t>(io.out0 + gbase) & 15) == 0);
 }
 
 // Permutation gather of one tile, indices local to the segment.
@@ -440,8 +441,8 @@ __global__ void __launch_bounds__(kThreads, 3)
       break;  // block-uniform; the abort flag releases any waiting block
     }
     if (task.kind == kTaskScan) {
-      scan_tile_task(seg, task.tile, io, sm.scan.tile, sm.scan.sh, &bar, phase,
-                     [&] { take_next(); });
+      scan_tile_task<TS32, kThreads, kChunks>(seg, task.tile, io, sm.scan.tile, sm.scan.sh, &bar, phase,
+                                     [&] { take_next(); });
     } else if (task.kind == kTaskGather) {
       take_next();
       gather_tile_task(seg, task.tile, io);
@@ -493,10 +494,16 @@ __global__ void __launch_bounds__(kThreads, 3)
 // Stream order separates the kinds, so no task waits on a flag; scan tiles
 // wait only on lower tiles of their own segment (lower block indices).
 
-__global__ void __launch_bounds__(kThreads, 6)
+// Scan tiles as the global look-back scan cuts them: 128 threads x 8
+// 16-byte chunks (the same 4096 elements), 10 blocks per SM (12 spilled
+// 52 bytes and ran 1.5% slower).
+constexpr int kScanThreads = 128, kScanChunks = 8;
+using TSK = TileScan<int32_t, kScanThreads, kScanChunks>;
+
+__global__ void __launch_bounds__(kScanThreads, 10)
     kind_scan_kernel(const DevSeg *__restrict__ segs, const DevTask *__restrict__ tasks, TaskIO io) {
   __shared__ alignas(128) int32_t tile[kTile];
-  __shared__ TS32::Shared sh;
+  __shared__ TSK::Shared sh;
   __shared__ alignas(8) uint64_t bar;
   if (threadIdx.x == 0) {
     mbar_init(&bar, 1);
@@ -510,7 +517,7 @@ __global__ void __launch_bounds__(kThreads, 6)
     return;
   }
   uint32_t phase = 0;
-  scan_tile_task(seg, task.tile, io, tile, sh, &bar, phase, [] {});
+  scan_tile_task<TSK, kScanThreads, kScanChunks>(seg, task.tile, io, tile, sh, &bar, phase, [] {});
 }
 
 __global__ void __launch_bounds__(kThreads, 8)
@@ -766,7 +773,8 @@ int edpp_batch_launch(const edpp_batch_plan *plan, const int32_t *in0, const int
                   p.num_segs};
   if (p.schedule == EDPP_BATCH_SCHEDULE_KINDS) {
     if (p.n_scan)
-      kind_scan_kernel<<<static_cast<unsigned>(p.n_scan), kThreads, 0, st>>>(dsegs, dtasks, io);
+      kind_scan_kernel<<<static_cast<unsigned>(p.n_scan), kScanThreads, 0, st>>>(dsegs, dtasks,
+                                                                                 io);
     if (p.n_gather)
       kind_gather_kernel<<<static_cast<unsigned>(p.n_gather), kThreads, 0, st>>>(
           dsegs, dtasks + p.n_scan, io);
