@@ -222,7 +222,7 @@ __device__ __forceinline__ void gather_tile_task(const DevSeg &seg, int tile, co
       idx[q] = i < count ? io.in1[gbase + i] : -1;
     }
 #pragma unroll
-    for (int q = 0; q < 4; ++q) v[q] = (idx[q] >= 0 && idx[q] < seg.len) ? __ldg(src + idx[q]) : 0;
+    for (int q = 0; q < 4; ++q) v[q] = (idx[q] >= 0 && idx[q] < seg.len) ? src[idx[q]] : 0;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const int i = (k + q) * kThreads + t;

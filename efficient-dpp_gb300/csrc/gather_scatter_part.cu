@@ -46,11 +46,9 @@ __device__ __forceinline__ unsigned lanemask_lt() {
   return m;
 }
 
-__device__ __forceinline__ int ld_nc(const int32_t *p) {
-  int v;
-  asm volatile("ld.global.nc.L1::no_allocate.b32 %0, [%1];" : "=r"(v) : "l"(p));
-  return v;
-}
+// Random read of a payload element: a plain global load (the read-only
+// .nc path measured much slower for random 4-byte reads on GB300).
+__device__ __forceinline__ int ld_random(const int32_t *p) { return *p; }
 
 // A slot for this lane's element among the tile's elements of window w (-1:
 // invalid): one shared-memory atomic per element.  Slots within a window come
@@ -458,7 +456,7 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
     for (int e = 0; e < kPer; ++e) {
       const bool valid = src[e].x >= 0;
-      pr[e] = make_int2(src[e].y, valid ? ld_nc(in + src[e].x) : 0);  // {i, value}
+      pr[e] = make_int2(src[e].y, valid ? ld_random(in + src[e].x) : 0);  // {i, value}
     }
 #pragma unroll
     for (int e = 0; e < kPer; ++e) {
@@ -1283,11 +1281,11 @@ int edpp_scatter_i32_tiled(const int32_t *in, int32_t *out, int64_t length, cons
 }
 
 int edpp_gather_prefers_direct(int64_t length) {
-  // A gather whose source is at most ~1.5x L2 keeps enough of it in L2 that
+  // A gather whose source is at most ~2.5x L2 keeps enough of it in L2 that
   // the direct random sweep wins (measured, int32 permutations: 2^25 0.49 ms
-  // direct against 0.59 ms tiled; 2^26 1.21 against 1.10; 2^27 2.79
-  // against 2.11; 2^28 5.6-6.0 against 4.3).
-  return static_cast<double>(length) * 4.0 <= 1.5 * static_cast<double>(edpp::device_l2_bytes());
+  // direct against 0.59 ms tiled; 2^26 1.00 against 1.10; 2^28 5.34
+  // against 4.32).
+  return static_cast<double>(length) * 4.0 <= 2.5 * static_cast<double>(edpp::device_l2_bytes());
 }
 
 }  // extern "C"

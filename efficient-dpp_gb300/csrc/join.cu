@@ -131,7 +131,7 @@ __global__ void __launch_bounds__(256)
     const uint32_t key = static_cast<uint32_t>(__ldg(keys + i));
     uint32_t h = np_slot(key, bits);
     unsigned long long e;
-    while ((e = __ldg(table + h)) != 0ull) {
+    while ((e = table[h]) != 0ull) {  // plain loads: random reads are slower on the .nc path
       if (static_cast<uint32_t>(e) == key) {
         matches += e >> 32;
         break;

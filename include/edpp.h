@@ -154,7 +154,7 @@ int edpp_scatter_i32_tiled(const int32_t *in, int32_t *out, int64_t length,
                            void *stream);
 /* 1 when a gather of `length` elements is faster as the direct single sweep
  * (edpp_gather_i32, pass 1) than in the tiled form on the current device: its
- * source is small enough (about 1.5x L2) to stay largely in L2.  Scatter
+ * source is small enough (about 2.5x L2) to stay largely in L2.  Scatter
  * always favours the tiled form. */
 int edpp_gather_prefers_direct(int64_t length);
 
