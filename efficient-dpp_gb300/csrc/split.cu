@@ -455,9 +455,11 @@ size_t split_pass_ws_bytes(int64_t n, int buckets) {
          edpp_scan_workspace_size(tiles * buckets, EDPP_I32, EDPP_SCAN_LOOKBACK);
 }
 
-// LSD workspace: temporary keys and values (8 bytes per element, any
-// layout), the bucket totals, then the passes' workspace.
-size_t lsd_tmp_bytes(int64_t n) { return round_up(static_cast<size_t>(n) * 8, 256); }
+// LSD workspace: temporary keys and values (two arrays of 4 bytes per
+// element, or {key,value} pairs over both), the bucket totals, then the
+// passes' workspace.
+size_t lsd_half_bytes(int64_t n) { return round_up(static_cast<size_t>(n) * 4, 256); }
+size_t lsd_tmp_bytes(int64_t n) { return 2 * lsd_half_bytes(n); }
 
 size_t split_ws_bytes(int64_t n, int buckets) {
   if (n <= 0 || buckets < 1) return 0;
@@ -528,9 +530,7 @@ int split_lsd(const int32_t *keys_in, int32_t *keys_out, int32_t *bucket_start, 
   char *w = static_cast<char *>(ws);
   const size_t tmp = lsd_tmp_bytes(n);
   int32_t *tk = reinterpret_cast<int32_t *>(w);  // keys, or {key,value} pairs
-  int32_t *tv = LAYOUT == EDPP_KVS_SOA
-                    ? reinterpret_cast<int32_t *>(w + round_up(static_cast<size_t>(n) * 4, 256))
-                    : nullptr;
+  int32_t *tv = LAYOUT == EDPP_KVS_SOA ? reinterpret_cast<int32_t *>(w + lsd_half_bytes(n)) : nullptr;
   int32_t *totals = reinterpret_cast<int32_t *>(w + tmp);
   const size_t used = tmp + round_up(static_cast<size_t>(buckets) * 4, 256);
   void *pws = w + used;
