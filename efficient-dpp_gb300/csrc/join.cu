@@ -19,7 +19,8 @@
 namespace edpp {
 namespace {
 
-constexpr int kThreads = 512;
+constexpr int kThreads = 1024;  // one block per SM (128 KB table): 32 warps hide its latency
+                                // (512 threads: 3.31 against 2.51 ms for 2^26 x 2^26)
 constexpr int kTableLog2 = 14;              // 16384 slots x 8 bytes = 128 KB
 constexpr int kTable = 1 << kTableLog2;
 constexpr int kChunk = kTable / 2;          // S tuples per build (load <= 0.5)
