@@ -112,8 +112,10 @@ __global__ void __launch_bounds__(kLbThreads, sizeof(T) == 4 ? 12 : 8)
 // ---- RTS / SSA building blocks ----------------------------------------------
 
 // Sum of in[lo, hi) by the whole block; the result is valid in thread 0.
-// lo is a multiple of the tile size (16-byte aligned when vec).
-template <typename T>
+// lo is a multiple of the tile size (16-byte aligned when vec).  kKeep: the
+// range is read again soon (the fused RTS), so its lines are loaded with the
+// normal L2 policy instead of evict-first.
+template <typename T, bool kKeep = false>
 __device__ __forceinline__ T block_reduce_range(const T *in, int64_t lo, int64_t hi, bool vec) {
   T acc = zero_of<T>();
   if (lo < hi) {
@@ -125,7 +127,7 @@ __device__ __forceinline__ T block_reduce_range(const T *in, int64_t lo, int64_t
       for (; i + 3 * kThreads < nv; i += 4 * kThreads) {
         Chunk<T> c[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) c[u].raw = __ldcs(p + i + u * kThreads);
+        for (int u = 0; u < 4; ++u) c[u].raw = kKeep ? __ldcg(p + i + u * kThreads) : __ldcs(p + i + u * kThreads);
 #pragma unroll
         for (int u = 0; u < 4; ++u)
 #pragma unroll
@@ -133,7 +135,7 @@ __device__ __forceinline__ T block_reduce_range(const T *in, int64_t lo, int64_t
       }
       for (; i < nv; i += kThreads) {
         Chunk<T> c;
-        c.raw = __ldcs(p + i);
+        c.raw = kKeep ? __ldcg(p + i) : __ldcs(p + i);
 #pragma unroll
         for (int e = 0; e < E; ++e) acc = op_add(acc, c.e[e]);
       }
@@ -198,7 +200,7 @@ template <typename T> __global__ void __launch_bounds__(1024) scan_partials_kern
 // Scan tiles [t_lo, t_hi) in order starting from `running`; returns the
 // running sum after the last tile (false: a bulk copy timed out).  `bar`
 // must be initialised; buffers and barriers are the caller's shared memory.
-template <typename T, bool kInclusive>
+template <typename T, bool kInclusive, bool kStreamOut = false>
 __device__ bool scan_tile_run(const T *in, T *out, int64_t n, int64_t t_lo, int64_t t_hi,
                               T &running, T (*buf)[TS<T>::kTile], typename TS<T>::Shared &sh,
                               uint64_t *bar, bool tma, bool vec_out, uint64_t timeout_ns,
@@ -234,7 +236,7 @@ __device__ bool scan_tile_run(const T *in, T *out, int64_t n, int64_t t_lo, int6
     }
     __syncthreads();
     S::template phase3<kInclusive>(c, wex, sh, running);
-    S::store(out, t * kTile, count, c, vec_out);
+    S::template store<kStreamOut>(out, t * kTile, count, c, vec_out);
     running = op_add(running, sh.total);
     bulk_cur = bulk_next;
     __syncthreads();  // everyone done with buf[slot] and sh before reuse
@@ -269,9 +271,10 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // One-launch reduce-then-scan for inputs that fit in L2: every block reduces
-// its run of tiles, the last block to finish scans the block sums, the others
-// wait for it (bounded), and every block then scans its tiles again, now from
-// L2.  Launched cooperatively, so all blocks are resident together.
+// its run of tiles (the lines stay in L2), the last block to publish its sum
+// releases the others (bounded wait), every block adds up the sums of the
+// blocks before it, then scans its tiles again from L2, streaming the output.
+// Launched cooperatively, so all blocks are resident together.
 template <typename T, bool kInclusive>
 __global__ void __launch_bounds__(kThreads)
     rts_fused_kernel(const T *in, T *out, int64_t n, int64_t tpb, T *partials, unsigned *ctl,
@@ -291,47 +294,22 @@ __global__ void __launch_bounds__(kThreads)
     mbar_init(&bar[1], 1);
     fence_mbar_init();
   }
-  // 1. block sum of my tiles
-  const T agg = t_lo < t_hi ? block_reduce_range(in, t_lo * kTile, min64(n, t_hi * kTile), tma)
-                            : zero_of<T>();
+  // 1. block sum of my tiles, their lines kept in L2 for the second read
+  const T agg = t_lo < t_hi
+                    ? block_reduce_range<T, true>(in, t_lo * kTile, min64(n, t_hi * kTile), tma)
+                    : zero_of<T>();
   if (tid == 0) {
     partials[blockIdx.x] = agg;
     __threadfence();
     s_last = atomicAdd(&ctl[0], 1u) + 1u == gridDim.x;
   }
   __syncthreads();
-  // 2. the last block scans the block sums (exclusive, in place) and releases the rest
-  if (s_last) {
+  // 2. the last block to publish its sum releases the others at once
+  if (s_last && tid == 0) {
     __threadfence();
-    const int m = static_cast<int>(gridDim.x);
-    const int per = (m + kThreads - 1) / kThreads;
-    const int lo = min(m, tid * per), hi = min(m, lo + per);
-    T sum = zero_of<T>();
-    for (int i = lo; i < hi; ++i) sum = op_add(sum, __ldcg(partials + i));
-    __shared__ T wsum[kThreads / 32];
-    const int lane = tid & 31, w = tid >> 5;
-    const T si = warp_incl_scan(sum, lane);
-    if (lane == 31) wsum[w] = si;
-    __syncthreads();
-    if (w == 0) {
-      const T x = lane < kThreads / 32 ? wsum[lane] : zero_of<T>();
-      const T xi = warp_incl_scan(x, lane);
-      const T ex = shfl_up(xi, 1);
-      if (lane < kThreads / 32) wsum[lane] = lane == 0 ? zero_of<T>() : ex;
-    }
-    __syncthreads();
-    const T ex_t = shfl_up(si, 1);
-    T run = op_add(wsum[w], lane == 0 ? zero_of<T>() : ex_t);
-    for (int i = lo; i < hi; ++i) {
-      const T v = __ldcg(partials + i);
-      partials[i] = run;
-      run = op_add(run, v);
-    }
-    __threadfence();
-    __syncthreads();
-    if (tid == 0) st_release_u32(&ctl[1], 1u);
+    st_release_u32(&ctl[1], 1u);
   }
-  // 3. wait for the block offsets (bounded)
+  // 3. wait for every block sum (bounded)
   if (tid == 0) {
     bool ok = ld_acquire_u32(&ctl[1]) != 0u;
     if (!ok) {
@@ -346,10 +324,24 @@ __global__ void __launch_bounds__(kThreads)
   }
   __syncthreads();
   if (!s_ok) return;
-  T running = __ldcg(partials + blockIdx.x);
+  // every block adds up the sums of the blocks before it itself (at most a
+  // few thousand values from L2), instead of one block scanning them all
+  // while the others wait
+  T pre = zero_of<T>();
+  for (int i = tid; i < static_cast<int>(blockIdx.x); i += kThreads)
+    pre = op_add(pre, __ldcg(partials + i));
+  __shared__ T s_pre[kThreads / 32];
+  pre = warp_sum(pre);
+  if ((tid & 31) == 0) s_pre[tid >> 5] = pre;
+  __syncthreads();
+  T running = zero_of<T>();
+#pragma unroll
+  for (int k = 0; k < kThreads / 32; ++k) running = op_add(running, s_pre[k]);
+  // 4. scan the tiles again from L2; the output streams out (evict-first),
+  // so it does not push the input's remaining lines out of L2
   if (t_lo < t_hi)
-    scan_tile_run<T, kInclusive>(in, out, n, t_lo, t_hi, running, buf, sh, bar, tma, vec_out,
-                                 timeout_ns, fault);
+    scan_tile_run<T, kInclusive, true>(in, out, n, t_lo, t_hi, running, buf, sh, bar, tma,
+                                       vec_out, timeout_ns, fault);
 }
 
 // SSA third pass: out[range of block b] += offsets[b].

@@ -259,7 +259,8 @@ template <typename T, int THREADS, int CHUNKS> struct TileScan {
   }
 
   // Store this thread's chunks to out[tile_base ...], `count` valid elements
-  // in the tile.  vec: out is 16-byte aligned.
+  // in the tile.  vec: out is 16-byte aligned.  kStream: evict-first stores.
+  template <bool kStream = false>
   __device__ __forceinline__ static void store(T *out, int64_t tile_base, int count,
                                                const Chunk<T> (&c)[CHUNKS], bool vec) {
     const int t = threadIdx.x;
@@ -267,7 +268,9 @@ template <typename T, int THREADS, int CHUNKS> struct TileScan {
     for (int k = 0; k < CHUNKS; ++k) {
       const int off = (k * THREADS + t) * E;
       if (vec && off + E <= count) {
-        reinterpret_cast<uint4 *>(out + tile_base)[k * THREADS + t] = c[k].raw;
+        uint4 *dst = reinterpret_cast<uint4 *>(out + tile_base) + k * THREADS + t;
+        if (kStream) __stcs(dst, c[k].raw);
+        else *dst = c[k].raw;
       } else {
 #pragma unroll
         for (int e = 0; e < E; ++e)
