@@ -128,3 +128,30 @@ def test_config5_batch_equals_plain_and_graph_replay(cuda, edpp, batch):
         cuda.cuda.synchronize()
         assert cuda.equal(q0, o0) and cuda.equal(q1, o1)
     assert edpp.sync_status() == edpp.EDPP_OK
+
+
+@pytest.mark.parametrize("seed", [101, 102, 103])
+def test_random_segment_tables_every_schedule(cuda, edpp, batch, seed):
+    # 300 segments of 0..131072 elements, random ops and split bucket counts,
+    # random gaps between segments (so some start off a 16-byte boundary);
+    # every schedule gives the oracle's arrays
+    rng = np.random.default_rng(seed)
+    num = 300
+    lengths = (2.0 ** rng.uniform(0, 17, num)).astype(np.int64)
+    lengths[rng.random(num) < 0.05] = 0
+    ops = rng.integers(0, 3, num)
+    segs = np.zeros(num, batch.SEG_DTYPE)
+    off = 0
+    for i in range(num):
+        off += int(rng.integers(0, 6))
+        b = int(2 ** rng.integers(0, 9)) if ops[i] == 1 else 0
+        segs[i] = (off, int(lengths[i]), int(ops[i]), b, 0)
+        off += int(lengths[i])
+    in0, in1 = batch.gen_inputs(segs, seed=seed)
+    e0, e1 = reference_outputs(segs, in0, in1)
+    for tu in (None, batch.Tuning(0, 0, 0, 0), batch.Tuning(2, 0, 1, 1), batch.Tuning(3, 2, 0, 1)):
+        o0, o1, _ = _run_batch(batch, cuda, segs, in0, in1, tu)
+        assert edpp.sync_status() == edpp.EDPP_OK
+        g0, g1 = _mask_unused(segs, to_host(o0), to_host(o1))
+        np.testing.assert_array_equal(g0, e0)
+        np.testing.assert_array_equal(g1, e1)
