@@ -982,11 +982,13 @@ __global__ void __launch_bounds__(kThreads, kRefineBlocksPerSm)
 // start, [f << fine_log, fill_end[f])) are {index, value} with index inside
 // the window; they are applied in shared memory and the written elements of
 // the window are stored (a bitmap marks them; untouched elements keep their
-// old value in `out`).
+// old value in `out`).  unique: no index repeats (a gather's return trip),
+// so a window with as many pairs as elements is written whole and needs no
+// bitmap.
 __global__ void __launch_bounds__(kWinThreads)
     win_apply_kernel(const int2 *__restrict__ pairs, const uint32_t *__restrict__ start,
                      const uint32_t *__restrict__ fill_end, int fine_log, int64_t n,
-                     int32_t *__restrict__ out, bool vec_out) {
+                     int32_t *__restrict__ out, bool vec_out, bool unique) {
   extern __shared__ __align__(16) int32_t win[];
   const int W = 1 << fine_log;
   uint32_t *bits = reinterpret_cast<uint32_t *>(win + W);
@@ -995,13 +997,15 @@ __global__ void __launch_bounds__(kWinThreads)
   const int len = static_cast<int>(min64(W, n - base));
   const int64_t lo = start ? start[f] : base;
   const int64_t hi = start ? start[f + 1] : fill_end[f];
+  const bool whole = unique && hi - lo == len;  // block-uniform
   const int t = threadIdx.x;
-  for (int i = t; i < (W >> 5); i += kWinThreads) bits[i] = 0u;
+  if (!whole)
+    for (int i = t; i < (W >> 5); i += kWinThreads) bits[i] = 0u;
   __syncthreads();
   auto put = [&](int2 p) {
     const int rel = static_cast<int>(p.x - base);
     win[rel] = p.y;
-    atomicOr(&bits[rel >> 5], 1u << (rel & 31));
+    if (!whole) atomicOr(&bits[rel >> 5], 1u << (rel & 31));
   };
   // pairs: scalar head to an even index, then two per 16-byte load
   int64_t j = lo;
@@ -1026,7 +1030,7 @@ __global__ void __launch_bounds__(kWinThreads)
   if (t == 0 && j + 2 * nv < hi) put(pairs[j + 2 * nv]);
   __syncthreads();
   for (int e0 = 4 * t; e0 < len; e0 += 4 * kWinThreads) {
-    const uint32_t nib = (bits[e0 >> 5] >> (e0 & 31)) & 0xFu;
+    const uint32_t nib = whole ? 0xFu : (bits[e0 >> 5] >> (e0 & 31)) & 0xFu;
     if (nib == 0xFu && vec_out && e0 + 3 < len) {
       __stcs(reinterpret_cast<int4 *>(out + base + e0), *reinterpret_cast<const int4 *>(win + e0));
     } else {
@@ -1219,7 +1223,7 @@ int tiled_run(const int32_t *in, int32_t *out, int64_t n, const int32_t *loc, in
       pa, start + p.F, nullptr, 0, p.fine_log, p.coarse_log, tiles, fill, pb, kDefaultWaitNs, fault);
   if (kScatter) {
     win_apply_kernel<<<static_cast<unsigned>(p.F), kWinThreads, apply_smem(p.fine_log), st>>>(
-        pb, start, nullptr, p.fine_log, n, out, aligned16(out));
+        pb, start, nullptr, p.fine_log, n, out, aligned16(out), false);
   } else {
     win_fetch_kernel<<<static_cast<unsigned>(p.F), kFetchThreads, fetch_smem(p.fine_log, p.C), st>>>(
         pb, start, in, n, p.fine_log, p.coarse_log, p.C, cfill2, pa, vec_in, kDefaultWaitNs, fault);
@@ -1228,7 +1232,7 @@ int tiled_run(const int32_t *in, int32_t *out, int64_t n, const int32_t *loc, in
         pa, nullptr, cfill2, p.coarse_log, p.fine_log, p.coarse_log, rtiles, fill2, pb,
         kDefaultWaitNs, fault);
     win_apply_kernel<<<static_cast<unsigned>(p.F), kWinThreads, apply_smem(p.fine_log), st>>>(
-        pb, nullptr, fill2, p.fine_log, n, out, aligned16(out));
+        pb, nullptr, fill2, p.fine_log, n, out, aligned16(out), true);
   }
   return launch_status();
 }
