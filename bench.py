@@ -579,7 +579,8 @@ def run_split_workload(args, rank, world):
     vals = torch.arange(n, dtype=torch.int32, device=dev)
     ko = torch.empty(n, dtype=torch.int32, device=dev)
     vo = torch.empty_like(ko)
-    ws = edpp.workspace(edpp.split_workspace_bytes(n, 4096, "soa"), dev)
+    blist0 = [int(b) for b in args.split_buckets.split(",")] if args.split_buckets else [4096]
+    ws = edpp.workspace(max(edpp.split_workspace_bytes(n, b, "soa") for b in blist0 + [4096]), dev)
     uniform = torch.from_numpy(edpp.gen_keys_uniform(n, 3)).to(dev)
     rows = []
     blist = [int(b) for b in args.split_buckets.split(",")] if args.split_buckets else \

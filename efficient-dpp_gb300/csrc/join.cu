@@ -157,9 +157,14 @@ int np_bits(int64_t build_len) {
   return bits;
 }
 
+constexpr int kMaxJoinBuckets = 8192;  // the split's limit
+
+// Partitions of at most half a build chunk of S tuples, up to 8192 of them
+// (2^26 uniform S tuples: 8192 partitions of one chunk each, so R's partition
+// is probed once).
 int auto_buckets(int64_t s_len) {
   int b = 1;
-  while (b < 4096 && s_len / b > kChunk / 2) b *= 2;  // a partition fills about half a build
+  while (b < kMaxJoinBuckets && s_len / b > kChunk / 2) b *= 2;
   return b;
 }
 
@@ -194,7 +199,7 @@ extern "C" {
 size_t edpp_hash_join_workspace_size(int64_t r_len, int64_t s_len, int buckets) {
   if (r_len < 0 || s_len < 0) return 0;
   if (buckets <= 0) buckets = edpp::auto_buckets(s_len);
-  if (buckets > 4096 || (buckets & (buckets - 1))) return 0;
+  if (buckets > edpp::kMaxJoinBuckets || (buckets & (buckets - 1))) return 0;
   return edpp::join_layout(r_len, s_len, buckets).bytes;
 }
 
@@ -205,7 +210,7 @@ int edpp_hash_join_count(const int32_t *r_keys, int64_t r_len, const int32_t *s_
   if (r_len < 0 || s_len < 0 || r_len > INT32_MAX || s_len > INT32_MAX || !d_count)
     return EDPP_EINVAL;
   if (buckets <= 0) buckets = auto_buckets(s_len);
-  if (buckets > 4096 || (buckets & (buckets - 1))) return EDPP_EINVAL;
+  if (buckets > kMaxJoinBuckets || (buckets & (buckets - 1))) return EDPP_EINVAL;
   cudaStream_t st = as_stream(stream);
   if (cudaMemsetAsync(d_count, 0, sizeof(unsigned long long), st) != cudaSuccess) return EDPP_ECUDA;
   if (r_len == 0 || s_len == 0) return EDPP_OK;

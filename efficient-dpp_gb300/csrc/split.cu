@@ -37,7 +37,8 @@ namespace edpp {
 namespace {
 
 constexpr int kTile = 8192;
-constexpr int kMaxBuckets = 4096;
+constexpr int kMaxBuckets = 8192;     // public limit; from 2048 on, two passes
+constexpr int kOnePassMax = 1024;     // largest bucket count one pass takes
 constexpr int kHistThreads = 512;
 constexpr int kDirectBuckets = 2;  // up to this many buckets the scatter writes from registers
 
@@ -57,7 +58,7 @@ template <int LAYOUT>
 __global__ void __launch_bounds__(kHistThreads)
     split_hist_kernel(const int32_t *__restrict__ keys, int64_t n, int buckets, int shift,
                       int64_t tiles, int32_t *__restrict__ his, bool vec) {
-  __shared__ uint32_t cnt[kMaxBuckets];
+  __shared__ uint32_t cnt[kOnePassMax];
   const unsigned mask = static_cast<unsigned>(buckets - 1);
   for (int b = threadIdx.x; b < buckets; b += kHistThreads) cnt[b] = 0;
   __syncthreads();
@@ -392,8 +393,7 @@ template <int THREADS, int LAYOUT> int set_smem_attr() {
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64) dev = 0;
   std::call_once(once[dev], [&] {
-    // 512 threads serve up to 1024 buckets, 256 threads the rest
-    const size_t bytes = scatter_smem_bytes<THREADS, LAYOUT>(THREADS == 512 ? 1024 : kMaxBuckets);
+    const size_t bytes = scatter_smem_bytes<THREADS, LAYOUT>(kOnePassMax);
     status[dev] = cuda_status(cudaFuncSetAttribute(split_scatter_kernel<THREADS, LAYOUT>,
                                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                    static_cast<int>(bytes)));
@@ -418,6 +418,7 @@ template <int LAYOUT>
 int split_layout(const int32_t *keys_in, int32_t *keys_out, int32_t *bucket_start, int64_t n,
                  int buckets, const int32_t *vals_in, int32_t *vals_out, void *ws, size_t ws_bytes,
                  cudaStream_t st, int shift = 0) {
+  if (buckets > kOnePassMax) return EDPP_EINVAL;  // callers take two passes from 2048 on
   const int64_t tiles = (n + kTile - 1) / kTile;
   int32_t *his = static_cast<int32_t *>(ws);
   const int64_t hlen = tiles * buckets;
@@ -435,10 +436,7 @@ int split_layout(const int32_t *keys_in, int32_t *keys_out, int32_t *bucket_star
     s = launch_status();
     if (s != EDPP_OK) return s;
   }
-  if (buckets <= 1024)
-    return launch_scatter<512, LAYOUT>(keys_in, keys_out, vals_in, vals_out, n, buckets, shift,
-                                       tiles, his, tma, st);
-  return launch_scatter<256, LAYOUT>(keys_in, keys_out, vals_in, vals_out, n, buckets, shift,
+  return launch_scatter<512, LAYOUT>(keys_in, keys_out, vals_in, vals_out, n, buckets, shift,
                                      tiles, his, tma, st);
 }
 

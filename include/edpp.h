@@ -195,7 +195,8 @@ size_t edpp_split_workspace_size(int64_t length, int buckets, int layout);
 
 /* Stable multi-split by bucket = key & (buckets-1): the output holds the
  * input's elements grouped by bucket in ascending bucket order, in input
- * order within a bucket.  buckets is a power of two in [1, 4096].
+ * order within a bucket.  buckets is a power of two in [1, 8192] (from 2048
+ * buckets the split runs as two stable passes, low 8 bits then the rest).
  * bucket_start (optional, int32[buckets]) receives the first output index of
  * every bucket, as gatherStartPos does (opencl/kernels/split_kernel.cl:320-332).
  * KO: keys_in/keys_out hold keys, vals_* are ignored.  KVS_SOA: keys and
@@ -240,7 +241,7 @@ int edpp_radix_sort_i32(const int32_t *keys_in, int32_t *keys_out,
 
 /* Number of pairs (r, s) with r_keys[r] == s_keys[s], written to *d_count
  * (device memory).  Both relations are split into `buckets` partitions by
- * key & (buckets-1) (power of two <= 4096; 0 = chosen from s_len), then one
+ * key & (buckets-1) (power of two <= 8192; 0 = chosen from s_len), then one
  * block per partition pair builds a shared-memory hash table from S and
  * probes it with R.  Counterpart of the reference's partitioned hash join,
  * which also returns only the match count (obsolete/OpenCL/phjImpl.cpp:14-129,

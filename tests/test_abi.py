@@ -50,12 +50,13 @@ def test_workspace_queries(edpp):
     assert lib.edpp_scan_workspace_size(1 << 24, 1, 0) > a  # int64 state is larger
     assert lib.edpp_split_workspace_size(1 << 20, 256, 2) > 0
     assert lib.edpp_split_workspace_size(1 << 20, 3, 2) == 0  # not a power of two
-    assert lib.edpp_split_workspace_size(1 << 20, 8192, 2) == 0  # beyond 4096
+    assert lib.edpp_split_workspace_size(1 << 20, 16384, 2) == 0  # beyond 8192
     # from 2048 buckets the split runs as two passes through a temporary copy
     # of keys and values (8 bytes per element) besides the passes' workspace
     n = 1 << 20
     assert lib.edpp_split_workspace_size(n, 2048, 2) >= 8 * n
     assert lib.edpp_split_workspace_size(n, 4096, 2) >= 8 * n
+    assert lib.edpp_split_workspace_size(n, 8192, 2) >= 8 * n
     assert lib.edpp_split_workspace_size(n, 1024, 2) < 8 * n
     # the tiled gather/scatter: two pair arrays of 8 bytes per element
     assert lib.edpp_gather_tiled_workspace_size(n) >= 16 * n

@@ -10,7 +10,7 @@ pytestmark = pytest.mark.gpu
 @pytest.mark.parametrize("r_len,s_len,key_range", [(1, 1, 10), (1000, 3000, 500),
                                                    (1 << 20, 1 << 20, 1 << 20),
                                                    ((1 << 22) + 7, (1 << 21) + 3, 1 << 23)])
-@pytest.mark.parametrize("buckets", [0, 1, 64, 4096, "np"])
+@pytest.mark.parametrize("buckets", [0, 1, 64, 4096, 8192, "np"])
 def test_uniform_keys(cuda, edpp, orc, r_len, s_len, key_range, buckets):
     r = edpp.gen_uniform_i32(r_len, 7, 0, key_range - 1)
     s = edpp.gen_uniform_i32(s_len, 8, 0, key_range - 1)

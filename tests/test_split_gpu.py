@@ -7,7 +7,7 @@ from conftest import to_dev, to_host
 
 pytestmark = pytest.mark.gpu
 
-BUCKETS = [1, 2, 4, 8, 16, 32, 64, 128, 256, 512, 1024, 2048, 4096]
+BUCKETS = [1, 2, 4, 8, 16, 32, 64, 128, 256, 512, 1024, 2048, 4096, 8192]
 
 
 def _run(edpp, keys, B, layout, vals=None, start=True):
@@ -39,7 +39,7 @@ def test_uniform_keys(cuda, edpp, orc, B, n, layout):
     np.testing.assert_array_equal(st, es)
 
 
-@pytest.mark.parametrize("B", [2, 64, 256, 1024, 2048, 4096])  # 2048+: two stable passes
+@pytest.mark.parametrize("B", [2, 64, 256, 1024, 2048, 4096, 8192])  # 2048+: two stable passes
 def test_zipf_keys_large(cuda, edpp, orc, B):
     n = (1 << 22) + 77
     keys = edpp.gen_keys_zipf(n, 3, B, 1.0)
