@@ -21,7 +21,7 @@ def test_counting_sort_equals_cuda_ballot_split(orc, edpp, bits, n):
     np.testing.assert_array_equal(ko, np.sort(keys))
 
 
-@pytest.mark.parametrize("buckets", [1, 2, 16, 256, 1024, 4096])
+@pytest.mark.parametrize("buckets", [1, 2, 16, 256, 1024, 4096, 8192])
 @pytest.mark.parametrize("n", [1, 38, 39, 1000, 100003])
 def test_counting_sort_equals_single_split(orc, edpp, buckets, n):
     keys = edpp.gen_keys_uniform(n, 3)
