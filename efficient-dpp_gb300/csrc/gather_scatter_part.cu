@@ -773,10 +773,17 @@ __global__ void __launch_bounds__(1024)
                     uint32_t *__restrict__ cfill2) {
   __shared__ uint32_t wsum[32];
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-  const int per = (F + 1023) / 1024;
+  const int per = (F + 1023) / 1024;  // <= kMaxFine / 1024
   const int lo = min(F, t * per), hi = min(F, lo + per);
+  // all of this thread's counts are loaded at once and kept in registers
+  constexpr int kPerMax = kMaxFine / 1024;
+  uint32_t v[kPerMax];
   uint32_t s = 0;
-  for (int i = lo; i < hi; ++i) s += cnt[i];
+#pragma unroll
+  for (int k = 0; k < kPerMax; ++k) {
+    v[k] = lo + k < hi ? cnt[lo + k] : 0u;
+    s += v[k];
+  }
   uint32_t incl = s;
 #pragma unroll
   for (int d = 1; d < 32; d <<= 1) {
@@ -798,11 +805,15 @@ __global__ void __launch_bounds__(1024)
   }
   __syncthreads();
   uint32_t run = wsum[w] + incl - s;
-  for (int i = lo; i < hi; ++i) {
-    start[i] = run;
-    fill[i] = run;
-    if ((i & ((1 << kCoarseLogFan) - 1)) == 0) cfill[i >> kCoarseLogFan] = run;
-    run += cnt[i];
+#pragma unroll
+  for (int k = 0; k < kPerMax; ++k) {
+    const int i = lo + k;
+    if (i < hi) {
+      start[i] = run;
+      fill[i] = run;
+      if ((i & ((1 << kCoarseLogFan) - 1)) == 0) cfill[i >> kCoarseLogFan] = run;
+      run += v[k];
+    }
   }
   if (fill2) {
     for (int i = t; i < F; i += 1024) fill2[i] = static_cast<uint32_t>(i) << fine_log;
