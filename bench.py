@@ -14,6 +14,11 @@ add / triad 12 B per element.
 Schedule: gather / scatter run the shared-memory-window form by default
 (--method tiled; "partition" = L2 windows, "sweep" = the reference's pass-by-
 pass schedule); results are identical for every pass count and schedule.
+The tiled form does not use the pass count: its windows are fixed by the
+shared-memory size, so the five gather (and five scatter) calls of a step run
+the same kernels on the same arrays five times; the p1..p16 entries are not
+five schedules.  The reference's pass-by-pass schedule is timed per pass
+count under `compare.sweep`.
 
 value     device-timed, inputs resident in HBM (CUDA events, max over ranks)
 e2e       same metric through the C ABI with host buffers: every step copies
@@ -23,9 +28,20 @@ roofline  the dominant call of the step against the measured HBM copy rate
 cpu_baseline  the reference's CPU path (OpenMP ports, oracle/) on the host
           cores, on a bounded sample; rank 0 at N=1 only
 
---impl reference runs the reference's CPU implementation of the same step
-(OpenMP ports of openmp/test_gather_scatter_CPU.cpp and
-openmp/test_bandwidth_CPU.cpp; add/triad restated) on all host threads.
+The same line also carries the other configurations as keys (skipped with
+--no-extras): config1_scan (2^24 int32 exclusive scan, warm and L2-flushed),
+config4_scan (2^30 int32 / int64 / f32 scans under the three schemes, with the
+f32 error against an f64 accumulation), config3_split (2^28 key/value stable
+split, 2..1024 buckets, uniform and Zipf keys), config5_batch (4096 uneven
+segments batched vs one plain call per segment, and the persistent work-queue
+form) and config5_serve (Poisson request stream, p50 / p99 latency).  Each has
+its own GB/s, fraction of HBM and, where the reference has a CPU path, its
+cpu_baseline.
+
+--impl reference runs the reference's CPU implementation of the same step at
+the same size (OpenMP ports of openmp/test_gather_scatter_CPU.cpp and
+openmp/test_bandwidth_CPU.cpp; add/triad restated) on all host threads; it
+loads only the oracle, never this library.
 
 Multi-GPU: the primitives do not shard (replicas only); under torchrun each
 rank runs the full step on its own GPU, value = all ranks' bytes / max time.
@@ -35,6 +51,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -194,10 +211,9 @@ def cpu_baseline(n_sample: int, reps: int = 5):
     sample; returns the same metric (GB/s) and a description."""
     import numpy as np
 
-    import edpp
     from oracle import oracle as orc
     threads = orc.max_threads()
-    loc = edpp.gen_permutation(n_sample, 2)
+    loc = orc.gen_permutation(n_sample, 2)
     inp = np.arange(n_sample, dtype=np.int32)
     a = np.arange(n_sample, dtype=np.float32)
     b = a + 10
@@ -224,16 +240,18 @@ def cpu_baseline(n_sample: int, reps: int = 5):
 
 
 def run_reference(args, rank, world):
-    """--impl reference: the reference's CPU implementation of the step."""
+    """--impl reference: the reference's CPU implementation of the step, at
+    the GPU arm's size (2^28 by default) on all host threads.  It loads only
+    the oracle (OpenMP ports of the reference's CPU functions and the seeded
+    permutation generator), never this library."""
     if rank != 0:
         return 0
     import numpy as np
 
-    import edpp
     from oracle import oracle as orc
-    n = args.ref_n
+    n = args.ref_n or (1 << args.log2n)
     threads = orc.max_threads()
-    loc = edpp.gen_permutation(n, 2)
+    loc = orc.gen_permutation(n, 2)
     inp = np.arange(n, dtype=np.int32)
     a = np.arange(n, dtype=np.float32)
     b = a + 10
@@ -263,12 +281,20 @@ def run_reference(args, rank, world):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32+f32", "data": "synthetic",
-        "config": {"workload": "multipass gather/scatter + STREAM", "n": n,
-                   "passes": list(PASSES), "note": "reference CPU path on a bounded sample"},
+        "config": {"workload": "multipass gather/scatter (2^28 int32, Fisher-Yates seed 2, "
+                               "passes 1,2,4,8,16) + STREAM copy/scale/add/triad "
+                               "(2^28 f32, scalar 3.0)" if n == 1 << 28 else
+                               f"multipass gather/scatter + STREAM at n={n}",
+                   "n": n, "passes": list(PASSES),
+                   "note": "reference CPU path, same arrays and sizes as the GPU arm"},
         "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": threads,
                          "kind": "port",
-                         "sample": f"n=2^{n.bit_length() - 1} per step (reference tree absent on "
-                                   f"this host: OpenMP ports of its CPU functions)"},
+                         "sample": f"the whole step at n=2^{n.bit_length() - 1} (OpenMP ports of "
+                                   f"openmp/test_gather_scatter_CPU.cpp:24-41 and "
+                                   f"test_bandwidth_CPU.cpp:39-56; add/triad restated"
+                                   + ("; the reference's AVX2 sources do not build on this Arm "
+                                      "host)" if platform.machine() in ("aarch64", "arm64")
+                                      else ")")},
         "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -276,19 +302,23 @@ def run_reference(args, rank, world):
     return 0
 
 
-def run_batch_workload(args, rank, world):
+def _device(args):
+    import torch
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.set_device(dev)
+    return dev
+
+
+def measure_batch(args, dev, world, steps, warmup, autotune=False):
     """Config 5: 4096 uneven segments (scan / 64-bucket split / permutation
     gather, total <= 2^30 int32): the batched launches (tuned schedule,
-    captured in a CUDA graph) against one plain C-ABI call per segment.
-    Metric: elements/s."""
+    captured in a CUDA graph) and the persistent work-queue launch against
+    one plain C-ABI call per segment.  Returns the figures as a dict."""
     import numpy as np
     import torch
 
     import edpp
     from edpp import batch as B
-    edpp.lib()
-    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
-    torch.cuda.set_device(dev)
     segs = B.config5_segments(cap=1 << args.batch_log2_total)
     in0, in1 = B.gen_inputs(segs, seed=4)
     n = len(in0)
@@ -304,7 +334,7 @@ def run_batch_workload(args, rank, world):
 
     tuning = B.tuned(segs)
     tune_info = None
-    if args.autotune:
+    if autotune:
         plan0 = B.Plan(segs)
         ws0 = plan0.workspace(dev)
         tuning, tms = B.autotune(segs, d0, d1, o0, o1, ws0, reps=3)
@@ -317,7 +347,7 @@ def run_batch_workload(args, rank, world):
     pws = B.plain_workspace(segs, dev)
 
     def timed(fn, reps):
-        for _ in range(args.warmup):
+        for _ in range(warmup):
             fn()
         torch.cuda.synchronize()
         barrier(world)
@@ -330,7 +360,7 @@ def run_batch_workload(args, rank, world):
         torch.cuda.synchronize()
         return max_over_ranks(e0.elapsed_time(e1) / reps, world)
 
-    plain_ms = timed(lambda: B.run_plain(segs, d0, d1, q0, q1, pws), args.steps)
+    plain_ms = timed(lambda: B.run_plain(segs, d0, d1, q0, q1, pws), steps)
     # batched: capture one launch in a CUDA graph, replay it
     g = torch.cuda.CUDAGraph()
     side = torch.cuda.Stream()
@@ -340,9 +370,17 @@ def run_batch_workload(args, rank, world):
             plan.launch(d0, d1, o0, o1, ws)
     stream.wait_stream(side)
     with ClockSampler(int(dev.index or 0)) as clk:
-        batch_ms = timed(g.replay, args.steps)
-    stream_ms = timed(lambda: plan.launch(d0, d1, o0, o1, ws), args.steps)
+        batch_ms = timed(g.replay, steps)
+    stream_ms = timed(lambda: plan.launch(d0, d1, o0, o1, ws), steps)
     identical = bool(torch.equal(o0, q0) and torch.equal(o1, q1))
+    # the persistent work-queue schedule (one launch) on the same segments
+    qplan = B.Plan(segs, B.Tuning(4, 1, 0, B.SCHEDULE_QUEUE))
+    qws = qplan.workspace(dev)
+    qplan.upload(qws)
+    o0.zero_()
+    o1.zero_()
+    queue_ms = timed(lambda: qplan.launch(d0, d1, o0, o1, qws), steps)
+    queue_identical = bool(torch.equal(o0, q0) and torch.equal(o1, q1))
     if edpp.sync_status() != edpp.EDPP_OK:
         raise SystemExit("device fault in the batch workload")
     peak, peak_kind = measured_peak_gbs()
@@ -353,51 +391,69 @@ def run_batch_workload(args, rank, world):
     # (a split takes three: histogram, per-segment histogram scans, scatter)
     launches = (int(bool(ops["scan"])) + int(bool(ops["gather"])) + 3 * int(bool(ops["split"]))
                 if kinds else 1)
+    del d0, d1, o0, o1, q0, q1, ws, pws, qws
+    torch.cuda.empty_cache()
+    return {
+        "workload": "4096 segments, log-uniform 2^10..2^24 rescaled to <= 2^30 int32 (seed 4), "
+                    "ops scan / 64-bucket split / gather",
+        "segments": len(segs), "elements": elems, "ops": ops, "tasks": plan.num_tasks,
+        "tuning": tuning.as_dict() if tuning else "default (kinds)",
+        "plain": {"ms": round(plain_ms, 4), "elements/s": round(elems / (plain_ms * 1e-3), 1)},
+        "batched_graph": {"ms": round(batch_ms, 4), "elements/s": round(elems / (batch_ms * 1e-3), 1),
+                          "GB/s": round(gbs, 1), "frac_of_hbm": round(gbs / peak, 4)},
+        "batched_stream_launch_ms": round(stream_ms, 4),
+        "persistent_queue": {"ms": round(queue_ms, 4),
+                             "elements/s": round(elems / (queue_ms * 1e-3), 1),
+                             "speedup_vs_plain": round(plain_ms / queue_ms, 3),
+                             "identical_to_plain": queue_identical},
+        "speedup_vs_plain": round(plain_ms / batch_ms, 3),
+        "identical_to_plain": identical,
+        "autotune": tune_info,
+        "roofline": {"bound": "hbm", "achieved": round(gbs, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(gbs / peak, 4), "traffic": None,
+                     "kernel": "batch kernels (whole batch)", "peak_source": peak_kind},
+        "launches_per_batch": launches,
+        "clocks": clk.summary(),
+        "cpu_baseline": None,
+        "cpu_baseline_note": "the comparison north_star names is plain per-segment C-ABI calls "
+                             "on the same GPU (plain.ms)",
+    }
+
+
+def run_batch_workload(args, rank, world):
+    """--workload batch: config 5 alone, as one JSON line."""
+    import edpp
+    edpp.lib()
+    dev = _device(args)
+    r = measure_batch(args, dev, world, args.steps, args.warmup, autotune=args.autotune)
     if rank == 0:
-        print(json.dumps({
-            "metric": METRIC, "workload_metric": "batched elements/s (one launch per tile kind, "
-                                                 "graph-captured) vs plain per-segment launches",
-            "value": round(world * elems / (batch_ms * 1e-3), 1), "unit": "elements/s",
-            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": round(batch_ms, 4), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-            "config": {"workload": "4096 segments, log-uniform 2^10..2^24 rescaled to <= 2^30 "
-                                   "int32 (seed 4), ops scan / 64-bucket split / gather",
-                       "segments": len(segs), "elements": elems, "ops": ops,
-                       "tasks": plan.num_tasks, "tuning": tuning.as_dict() if tuning else "default"},
-            "plain": {"ms": round(plain_ms, 4), "elements/s": round(elems / (plain_ms * 1e-3), 1)},
-            "batched_graph": {"ms": round(batch_ms, 4), "GB/s": round(gbs, 1),
-                              "frac_of_hbm": round(gbs / peak, 4)},
-            "batched_stream_launch_ms": round(stream_ms, 4),
-            "speedup_vs_plain": round(plain_ms / batch_ms, 3),
-            "identical_to_plain": identical,
-            "autotune": tune_info,
-            "roofline": {"bound": "hbm", "achieved": round(gbs, 1), "peak": peak, "unit": "GB/s",
-                         "frac": round(gbs / peak, 4), "traffic": None,
-                         "kernel": "batch kernels (whole batch)",
-                         "peak_source": peak_kind},
-            "gpu_launches": launches * args.steps,
-            "clocks": clk.summary(),
-        }), flush=True)
+        line = {"metric": METRIC,
+                "workload_metric": "batched elements/s (one launch per tile kind, graph-captured) "
+                                   "vs plain per-segment launches",
+                "value": round(world * r["elements"] / (r["batched_graph"]["ms"] * 1e-3), 1),
+                "unit": "elements/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": r["batched_graph"]["ms"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "int32", "data": "synthetic",
+                "config": {"workload": r["workload"], "segments": r["segments"],
+                           "elements": r["elements"], "ops": r["ops"], "tasks": r["tasks"],
+                           "tuning": r["tuning"]},
+                "gpu_launches": r["launches_per_batch"] * args.steps}
+        line.update({k: v for k, v in r.items() if k not in line and k != "workload"})
+        print(json.dumps(line), flush=True)
     return 0
 
 
-def run_serve_workload(args, rank, world):
+def measure_serve(args, dev, rates, requests):
     """Config 5, serving: Poisson arrivals at swept rates of requests with
     log-uniform sizes 4K..64M elements (op scan / 64-bucket split / gather),
     host buffers in pinned memory, admission cap 40 GB of HBM, continuous
     batching; p50 / p99 latency (submit -> outputs in host memory)."""
     import numpy as np
-    import torch
 
     import edpp
     from edpp import batch as B
     from edpp import serve as S
-    edpp.lib()
-    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
-    torch.cuda.set_device(dev)
-    if rank != 0:
-        return 0
     npay = args.serve_payloads
     sizes, ops = [], []
     for i in range(npay):
@@ -422,8 +478,8 @@ def run_serve_workload(args, rank, world):
         st, _ = srv.wait(rid)
         assert st == 0
     with ClockSampler(int(dev.index or 0)) as clk:
-        for rate in [float(x) for x in args.rates.split(",")]:
-            n = args.serve_requests
+        for rate in rates:
+            n = requests
             gaps = rng.exponential(1.0 / rate, size=n)
             arrivals = np.cumsum(gaps)
             inflight = {}
@@ -459,17 +515,29 @@ def run_serve_workload(args, rank, world):
                             "queue_p99_ms": round(float(np.percentile(queue, 99)), 3)})
     stats = srv.stats()
     srv.close()
-    best = max(results, key=lambda r: r["elements/s"])
+    return {"workload": "Poisson arrivals, sizes log-uniform 2^12..2^26 int32, ops scan / "
+                        "64-bucket split / gather, pinned host buffers",
+            "payloads": npay, "pool_bytes": int(args.pool_gb * 1e9), "slots": args.serve_slots,
+            "rates": results, "server": stats, "clocks": clk.summary()}
+
+
+def run_serve_workload(args, rank, world):
+    """--workload serve: the serving sweep alone, as one JSON line."""
+    import edpp
+    edpp.lib()
+    dev = _device(args)
+    if rank != 0:
+        return 0
+    r = measure_serve(args, dev, [float(x) for x in args.rates.split(",")], args.serve_requests)
+    best = max(r["rates"], key=lambda x: x["elements/s"])
     print(json.dumps({
         "metric": METRIC, "workload_metric": "served elements/s with p50/p99 latency",
         "value": best["elements/s"], "unit": "elements/s", "n_gpus": world,
-        "steps": len(results), "warmup": 1, "ms_per_step": None, "higher_is_better": True,
+        "steps": len(r["rates"]), "warmup": 1, "ms_per_step": None, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-        "config": {"workload": "Poisson arrivals, sizes log-uniform 2^12..2^26 int32, ops scan / "
-                               "64-bucket split / gather, pinned host buffers",
-                   "payloads": npay, "pool_bytes": int(args.pool_gb * 1e9),
-                   "slots": args.serve_slots},
-        "rates": results, "server": stats, "clocks": clk.summary(),
+        "config": {"workload": r["workload"], "payloads": r["payloads"],
+                   "pool_bytes": r["pool_bytes"], "slots": r["slots"]},
+        "rates": r["rates"], "server": r["server"], "clocks": r["clocks"],
         "e2e": {"value": best["elements/s"], "unit": "elements/s",
                 "note": "every request copies inputs host->device and outputs back"},
     }), flush=True)
@@ -499,116 +567,208 @@ def _event_ms(fn, reps, warmup, flush=None):
     return total / reps
 
 
-def run_scan_workload(args, rank, world):
+def _hampel_ms(fn, reps):
+    from oracle import oracle as orc
+    return orc.average_hampel([fn() for _ in range(reps)])
+
+
+FP32_EPS = 1.0  # relative error of an f32 scan: |gpu - f64| / max(|f64|, FP32_EPS)
+
+
+def measure_scans(args, dev, reps, warmup, config1=True, config4=True, cpu=True):
     """Configs 1 and 4: int32 exclusive scan of 2^24 values in [0,15]
     (seed 1), warm and with L2 flushed; global scans of 2^30 int32 / int64
     (inclusive and exclusive, values in [0,100], seed 1) and f32 inclusive
-    (values in [-1,1], seed 1) under the three schemes."""
+    (values in [-1,1], seed 1) under the three schemes, with the f32 result's
+    error against an f64 accumulation of the same inputs (the oracle).
+    cpu: the OpenMP ports of scan_SSA_omp / scan_RTS_omp on the host cores
+    (config 1 at full size, config 4 on a 2^28 sample)."""
     import numpy as np
     import torch
 
     import edpp
-    edpp.lib()
-    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
-    torch.cuda.set_device(dev)
     peak, peak_kind = measured_peak_gbs()
+    out = {"peak": peak, "peak_source": peak_kind}
     rows = []
-    flush = torch.empty(64 << 20, dtype=torch.int32, device=dev)  # 256 MB > L2
-    x24 = torch.from_numpy(edpp.gen_uniform_i32(1 << 24, 1, 0, 15)).to(dev)
-    y24 = torch.empty_like(x24)
-    for algo in ("lookback", "rts", "ssa"):
-        ws = edpp.workspace(edpp.scan_workspace_bytes(1 << 24, "int32", algo), dev)
-        for l2 in ("warm", "flushed"):
-            ms = _event_ms(lambda: edpp.scan(x24, algo=algo, out=y24, ws=ws), args.steps,
-                           args.warmup, flush if l2 == "flushed" else None)
-            gbs = 8 * (1 << 24) / (ms * 1e-3) / 1e9
-            rows.append({"config": "1", "n": 1 << 24, "dtype": "int32", "inclusive": False,
-                         "algo": algo, "l2": l2, "ms": round(ms, 4), "GB/s": round(gbs, 1),
-                         "frac_of_hbm": round(gbs / peak, 4)})
-    del x24, y24
-    n = 1 << args.scan_log2n
-    for dt, bpe in (() if args.scan_config1_only else
-                    (("int32", 8), ("int64", 16), ("float32", 8))):
-        if dt == "int32":
-            x = torch.from_numpy(edpp.gen_uniform_i32(n, 1, 0, 100)).to(dev)
-        elif dt == "int64":
-            x = torch.from_numpy(edpp.gen_uniform_i64(n, 1, 0, 100)).to(dev)
-        else:
-            x = torch.from_numpy(edpp.gen_uniform_f32(n, 1, -1.0, 1.0)).to(dev)
-        y = torch.empty_like(x)
-        for inc in ((False, True) if dt != "float32" else (True,)):
-            for algo in ("lookback", "rts", "ssa"):
-                ws = edpp.workspace(edpp.scan_workspace_bytes(n, dt, algo), dev)
-                ms = _event_ms(lambda: edpp.scan(x, inclusive=inc, algo=algo, out=y, ws=ws),
-                               args.steps, args.warmup)
-                gbs = bpe * n / (ms * 1e-3) / 1e9
-                rows.append({"config": "4", "n": n, "dtype": dt, "inclusive": inc, "algo": algo,
-                             "ms": round(ms, 4), "GB/s": round(gbs, 1),
+    if config1:
+        flush = torch.empty(64 << 20, dtype=torch.int32, device=dev)  # 256 MB > L2
+        h24 = edpp.gen_uniform_i32(1 << 24, 1, 0, 15)
+        x24 = torch.from_numpy(h24).to(dev)
+        y24 = torch.empty_like(x24)
+        for algo in ("lookback", "rts", "ssa"):
+            ws = edpp.workspace(edpp.scan_workspace_bytes(1 << 24, "int32", algo), dev)
+            for l2 in ("warm", "flushed"):
+                ms = _event_ms(lambda: edpp.scan(x24, algo=algo, out=y24, ws=ws), reps,
+                               warmup, flush if l2 == "flushed" else None)
+                gbs = 8 * (1 << 24) / (ms * 1e-3) / 1e9
+                rows.append({"config": "1", "n": 1 << 24, "dtype": "int32", "inclusive": False,
+                             "algo": algo, "l2": l2, "ms": round(ms, 4), "GB/s": round(gbs, 1),
                              "frac_of_hbm": round(gbs / peak, 4)})
-                del ws
-        del x, y
-        torch.cuda.empty_cache()
+        del x24, y24, flush
+        if cpu:
+            from oracle import oracle as orc
+            th = orc.max_threads()
+            c1 = {}
+            for scheme in ("ssa", "rts"):
+                ms = _hampel_ms(lambda: orc.scan_omp(h24, scheme, th)[1], 5)
+                c1[scheme] = {"ms": round(ms, 3),
+                              "GB/s": round(8 * (1 << 24) / (ms * 1e-3) / 1e9, 2)}
+            out["config1_cpu_baseline"] = {
+                "value": max(v["GB/s"] for v in c1.values()), "unit": "GB/s", "cores": th,
+                "kind": "port", "per_scheme": c1,
+                "sample": "the full config (2^24 int32); OpenMP ports of scan_SSA_omp / "
+                          "scan_RTS_omp (openmp/test_scan_CPU.cpp:85-163); Hampel mean of 5"}
+    if config4:
+        n = 1 << args.scan_log2n
+        fp32_err = {}
+        for dt, bpe in (("int32", 8), ("int64", 16), ("float32", 8)):
+            if dt == "int32":
+                h = edpp.gen_uniform_i32(n, 1, 0, 100)
+            elif dt == "int64":
+                h = edpp.gen_uniform_i64(n, 1, 0, 100)
+            else:
+                h = edpp.gen_uniform_f32(n, 1, -1.0, 1.0)
+            x = torch.from_numpy(h).to(dev)
+            y = torch.empty_like(x)
+            ref = None
+            if dt == "float32":
+                from oracle import oracle as orc
+                ref = torch.from_numpy(orc.scan(h, True)).to(dev)  # f64 accumulation
+            for inc in ((False, True) if dt != "float32" else (True,)):
+                for algo in ("lookback", "rts", "ssa"):
+                    ws = edpp.workspace(edpp.scan_workspace_bytes(n, dt, algo), dev)
+                    ms = _event_ms(lambda: edpp.scan(x, inclusive=inc, algo=algo, out=y, ws=ws),
+                                   reps, warmup)
+                    gbs = bpe * n / (ms * 1e-3) / 1e9
+                    rows.append({"config": "4", "n": n, "dtype": dt, "inclusive": inc,
+                                 "algo": algo, "ms": round(ms, 4), "GB/s": round(gbs, 1),
+                                 "frac_of_hbm": round(gbs / peak, 4)})
+                    if ref is not None:
+                        err = (y.double() - ref).abs_() / ref.abs().clamp_min(FP32_EPS)
+                        fp32_err[algo] = {"max_rel": float(err.max()),
+                                          "mean_rel": float(err.mean()),
+                                          "max_abs": float((y.double() - ref).abs().max())}
+                        del err
+                    del ws
+            del x, y, ref
+            torch.cuda.empty_cache()
+        out["fp32_inclusive_error"] = {
+            "n": n, "values": "uniform [-1,1], seed 1",
+            "definition": f"|gpu - f64| / max(|f64|, {FP32_EPS}) over all n outputs, f64 = "
+                          "sequential f64 accumulation of the same f32 inputs (the oracle)",
+            "per_scheme": fp32_err}
+        if cpu:
+            from oracle import oracle as orc
+            th = orc.max_threads()
+            ns = min(n, 1 << 28)
+            hs = edpp.gen_uniform_i32(ns, 1, 0, 100)
+            c4 = {}
+            for scheme in ("ssa", "rts"):
+                ms = _hampel_ms(lambda: orc.scan_omp(hs, scheme, th)[1], 3)
+                c4[scheme] = {"ms": round(ms, 3), "GB/s": round(8 * ns / (ms * 1e-3) / 1e9, 2)}
+            out["config4_cpu_baseline"] = {
+                "value": max(v["GB/s"] for v in c4.values()), "unit": "GB/s", "cores": th,
+                "kind": "port", "per_scheme": c4,
+                "sample": f"int32 exclusive at n=2^{ns.bit_length() - 1} of the 2^30 config; "
+                          "OpenMP ports of scan_SSA_omp / scan_RTS_omp; Hampel mean of 3"}
     if edpp.sync_status() != edpp.EDPP_OK:
         raise SystemExit("device fault in the scan workload")
-    head = [r for r in rows if r["config"] == "1" and r["algo"] == "lookback" and r["l2"] == "flushed"][0]
+    out["rows"] = rows
+    return out
+
+
+def run_scan_workload(args, rank, world):
+    """--workload scan: configs 1 and 4 alone, as one JSON line."""
+    import edpp
+    edpp.lib()
+    dev = _device(args)
+    r = measure_scans(args, dev, args.steps, args.warmup, config4=not args.scan_config1_only,
+                      cpu=not args.no_cpu)
+    rows = r["rows"]
+    head = [x for x in rows if x["config"] == "1" and x["algo"] == "lookback"
+            and x["l2"] == "flushed"][0]
     if rank == 0:
-        print(json.dumps({"metric": METRIC, "workload_metric": "scan GB/s (8 B/elem int32)",
-                          "value": head["GB/s"], "unit": "GB/s", "n_gpus": world,
-                          "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["ms"],
-                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                          "dtype": "int32", "data": "synthetic", "peak": peak,
-                          "peak_source": peak_kind,
-                          "config": {"workload": "scans: config 1 (2^24 int32 [0,15] seed 1) "
-                                                 "and config 4 (2^30, three schemes)"},
-                          "rows": rows}), flush=True)
+        line = {"metric": METRIC, "workload_metric": "scan GB/s (8 B/elem int32)",
+                "value": head["GB/s"], "unit": "GB/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["ms"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "int32", "data": "synthetic",
+                "config": {"workload": "scans: config 1 (2^24 int32 [0,15] seed 1) "
+                                       "and config 4 (2^30, three schemes)"}}
+        line.update(r)
+        print(json.dumps(line), flush=True)
     return 0
 
 
-def run_split_workload(args, rank, world):
+def measure_split(args, dev, reps, warmup, buckets, kinds=("uniform", "zipf"), cpu=True):
     """Config 3: stable split of 2^28 (int32 key, int32 value = index) pairs,
-    B = 2..1024, keys uniform over [0,2^31) or Zipf(1.0) buckets (seed 3)."""
-    import numpy as np
+    keys uniform over [0,2^31) or Zipf(1.0) buckets (seed 3).  cpu: the
+    stable split restatement (counting sort; the reference has no CPU
+    split) on a 2^24 sample at 256 buckets."""
     import torch
 
     import edpp
-    edpp.lib()
-    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
-    torch.cuda.set_device(dev)
     peak, peak_kind = measured_peak_gbs()
     n = 1 << args.split_log2n
     vals = torch.arange(n, dtype=torch.int32, device=dev)
     ko = torch.empty(n, dtype=torch.int32, device=dev)
     vo = torch.empty_like(ko)
-    blist0 = [int(b) for b in args.split_buckets.split(",")] if args.split_buckets else [4096]
-    ws = edpp.workspace(max(edpp.split_workspace_bytes(n, b, "soa") for b in blist0 + [4096]), dev)
-    uniform = torch.from_numpy(edpp.gen_keys_uniform(n, 3)).to(dev)
+    ws = edpp.workspace(max(edpp.split_workspace_bytes(n, b, "soa") for b in buckets), dev)
+    h_uniform = edpp.gen_keys_uniform(n, 3)
+    uniform = torch.from_numpy(h_uniform).to(dev)
     rows = []
-    blist = [int(b) for b in args.split_buckets.split(",")] if args.split_buckets else \
-        [2 ** k for k in range(1, 11)]
-    for B in blist:
-        for kind in ("uniform", "zipf"):
+    for B in buckets:
+        for kind in kinds:
             keys = uniform if kind == "uniform" else \
                 torch.from_numpy(edpp.gen_keys_zipf(n, 3, B, 1.0)).to(dev)
             ms = _event_ms(lambda: edpp.split(keys, B, values=vals, keys_out=ko, values_out=vo,
-                                              ws=ws), args.steps, args.warmup)
+                                              ws=ws), reps, warmup)
             gbs = 16 * n / (ms * 1e-3) / 1e9
             rows.append({"buckets": B, "keys": kind, "ms": round(ms, 4), "GB/s": round(gbs, 1),
                          "frac_of_hbm": round(gbs / peak, 4)})
-            if kind == "zipf":
+            if kind != "uniform":
                 del keys
     if edpp.sync_status() != edpp.EDPP_OK:
         raise SystemExit("device fault in the split workload")
-    head = ([r for r in rows if r["buckets"] == 256 and r["keys"] == "uniform"] or rows)[0]
+    out = {"workload": f"split 2^{args.split_log2n} KV (value = index), uniform / Zipf(1.0) keys, "
+                       "seed 3", "n": n, "peak": peak, "peak_source": peak_kind, "rows": rows}
+    del vals, ko, vo, ws, uniform
+    torch.cuda.empty_cache()
+    if cpu:
+        import numpy as np
+
+        from oracle import oracle as orc
+        ns = min(n, 1 << 24)
+        hk = h_uniform[:ns]
+        hv = np.arange(ns, dtype=np.int32)
+        ms = _hampel_ms(lambda: orc.split_timed(hk, 256, hv, "soa")[2], 3)
+        out["cpu_baseline"] = {
+            "value": round(16 * ns / (ms * 1e-3) / 1e9, 2), "unit": "GB/s", "cores": 1,
+            "kind": "restatement",
+            "sample": f"256 buckets, uniform keys, n=2^{ns.bit_length() - 1}; the reference has "
+                      "no CPU split: a single-thread counting-sort restatement, labelled as such"}
+    return out
+
+
+def run_split_workload(args, rank, world):
+    """--workload split: config 3 alone, as one JSON line."""
+    import edpp
+    edpp.lib()
+    dev = _device(args)
+    blist = [int(b) for b in args.split_buckets.split(",")] if args.split_buckets else \
+        [2 ** k for k in range(1, 11)]
+    r = measure_split(args, dev, args.steps, args.warmup, blist, cpu=not args.no_cpu)
+    rows = r["rows"]
+    head = ([x for x in rows if x["buckets"] == 256 and x["keys"] == "uniform"] or rows)[0]
     if rank == 0:
-        print(json.dumps({"metric": METRIC, "workload_metric": "stable split GB/s (16 B/pair)",
-                          "value": head["GB/s"], "unit": "GB/s", "n_gpus": world,
-                          "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["ms"],
-                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                          "dtype": "int32", "data": "synthetic", "peak": peak,
-                          "peak_source": peak_kind,
-                          "config": {"workload": f"split 2^{args.split_log2n} KV, B=2..1024, "
-                                                 "uniform / Zipf(1.0) keys, seed 3"},
-                          "rows": rows}), flush=True)
+        line = {"metric": METRIC, "workload_metric": "stable split GB/s (16 B/pair)",
+                "value": head["GB/s"], "unit": "GB/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["ms"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "int32", "data": "synthetic",
+                "config": {"workload": r["workload"]}}
+        line.update({k: v for k, v in r.items() if k != "workload"})
+        print(json.dumps(line), flush=True)
     return 0
 
 
@@ -794,10 +954,15 @@ def main(argv=None):
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="edpp", choices=["edpp", "reference"])
     ap.add_argument("--log2n", type=int, default=28)
-    ap.add_argument("--ref-n", type=int, default=1 << 26, help="reference arm sample size")
+    ap.add_argument("--ref-n", type=int, default=0,
+                    help="reference arm size (default: 2^log2n, the GPU arm's size)")
     ap.add_argument("--cpu-sample", type=int, default=1 << 26)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="default run: skip the config 1/3/4/5 keys (scan, split, batch, serve)")
+    ap.add_argument("--extras-serve-requests", type=int, default=200,
+                    help="default run: requests per rate of the serving sweep")
     ap.add_argument("--method", default="tiled", choices=["partition", "sweep", "tiled"],
                     help="gather/scatter schedule of the timed step")
     ap.add_argument("--no-compare", action="store_true",
@@ -1071,6 +1236,33 @@ def main(argv=None):
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline(args.cpu_sample)
 
+    # ---- the other configurations, each as its own key of the same line -------
+    # (not part of `value`, which stays the config-2 step above)
+    extras = {}
+    if not args.no_extras:
+        del d_loc, d_in, d_a, d_b, d_out, d_fout, ws
+        torch.cuda.empty_cache()
+        reps = max(3, min(args.steps, 5))
+        with_cpu = rank == 0 and world == 1 and not args.no_cpu
+        scans = measure_scans(args, dev, reps, args.warmup, cpu=with_cpu)
+        c1 = [r for r in scans["rows"] if r["config"] == "1"]
+        c4 = [r for r in scans["rows"] if r["config"] == "4"]
+        extras["config1_scan"] = {
+            "workload": "int32 exclusive scan, 2^24 values uniform in [0,15], seed 1",
+            "rows": c1, "cpu_baseline": scans.get("config1_cpu_baseline")}
+        extras["config4_scan"] = {
+            "workload": f"global scans at 2^{args.scan_log2n}: int32/int64 exclusive and "
+                        "inclusive (values in [0,100]), f32 inclusive ([-1,1]), seed 1, "
+                        "look-back / reduce-then-scan / scan-then-propagate",
+            "rows": c4, "fp32_inclusive_error": scans.get("fp32_inclusive_error"),
+            "cpu_baseline": scans.get("config4_cpu_baseline")}
+        extras["config3_split"] = measure_split(args, dev, reps, args.warmup,
+                                                [2 ** k for k in range(1, 11)], cpu=with_cpu)
+        extras["config5_batch"] = measure_batch(args, dev, world, reps, args.warmup)
+        if rank == 0:
+            extras["config5_serve"] = measure_serve(
+                args, dev, [float(x) for x in args.rates.split(",")], args.extras_serve_requests)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": "GB/s", "n_gpus": world,
@@ -1091,6 +1283,7 @@ def main(argv=None):
             "e2e": e2e,
             "cpu_baseline": cpu,
         }
+        line.update(extras)
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist

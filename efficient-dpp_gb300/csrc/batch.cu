@@ -757,6 +757,9 @@ int edpp_batch_launch(const edpp_batch_plan *plan, const int32_t *in0, const int
   if (ws_bytes < p.bytes) return EDPP_ENOMEM;
   if (p.tasks.empty()) return EDPP_OK;
   if (!in0 || !out0) return EDPP_EINVAL;
+  // gather tiles read in1 (indices); split tiles read in1 and write out1 (values)
+  if ((p.n_gather || p.n_split) && !in1) return EDPP_EINVAL;
+  if (p.n_split && !out1) return EDPP_EINVAL;
   unsigned *fault = fault_word();
   if (!fault) return EDPP_ECUDA;
   cudaStream_t st = as_stream(stream);
@@ -813,6 +816,23 @@ int edpp_batch_launch(const edpp_batch_plan *plan, const int32_t *in0, const int
 }  // extern "C"
 
 // ---- plain per-array launches (the baseline the batch replaces) ---------------
+namespace {
+constexpr int kNeedIn0Out0 = 1, kNeedIn1 = 2, kNeedOut1 = 4;
+// Which of the caller's arrays the segments touch: every non-empty segment
+// reads in0 and writes out0; gathers read in1 (indices); splits read in1
+// and write out1 (values).
+int batch_io_needs(const edpp_segment *segs, int num_segs) {
+  int need = 0;
+  for (int i = 0; i < num_segs; ++i) {
+    if (segs[i].length <= 0) continue;
+    need |= kNeedIn0Out0;
+    if (segs[i].op == EDPP_BATCH_GATHER) need |= kNeedIn1;
+    if (segs[i].op == EDPP_BATCH_SPLIT) need |= kNeedIn1 | kNeedOut1;
+  }
+  return need;
+}
+}  // namespace
+
 extern "C" size_t edpp_batch_plain_workspace_size(const edpp_segment *segs, int num_segs) {
   size_t m = 0;
   for (int i = 0; i < num_segs; ++i) {
@@ -832,6 +852,11 @@ extern "C" size_t edpp_batch_plain_workspace_size(const edpp_segment *segs, int 
 extern "C" int edpp_batch_run_plain(const edpp_segment *segs, int num_segs, const int32_t *in0,
                                     const int32_t *in1, int32_t *out0, int32_t *out1, void *ws,
                                     size_t ws_bytes, void *stream) {
+  if (num_segs > 0 && !segs) return EDPP_EINVAL;
+  const int need = batch_io_needs(segs, num_segs);
+  if ((need & kNeedIn0Out0) && (!in0 || !out0)) return EDPP_EINVAL;
+  if ((need & kNeedIn1) && !in1) return EDPP_EINVAL;
+  if ((need & kNeedOut1) && !out1) return EDPP_EINVAL;
   for (int i = 0; i < num_segs; ++i) {
     const edpp_segment &s = segs[i];
     if (s.length == 0) continue;
@@ -863,6 +888,11 @@ extern "C" int edpp_batch_autotune(const edpp_segment *segs, int num_segs, const
                                    size_t ws_bytes, void *stream, int reps,
                                    edpp_batch_tuning *best, float *best_ms) {
   if (!best || reps < 1) return EDPP_EINVAL;
+  if (num_segs > 0 && !segs) return EDPP_EINVAL;
+  const int need = batch_io_needs(segs, num_segs);
+  if ((need & kNeedIn0Out0) && (!in0 || !out0)) return EDPP_EINVAL;
+  if ((need & kNeedIn1) && !in1) return EDPP_EINVAL;
+  if ((need & kNeedOut1) && !out1) return EDPP_EINVAL;
   cudaStream_t st = edpp::as_stream(stream);
   cudaEvent_t a, b;
   if (cudaEventCreate(&a) != cudaSuccess) return EDPP_ECUDA;

@@ -540,11 +540,11 @@ int edpp_selftest_lookback_timeout(const int32_t *in, int32_t *out, int64_t leng
 }  // extern "C"
 
 // ---- allocation-free exclusive scan -------------------------------------------
-// For callers that cannot allocate device memory: code running where
-// cudaMalloc is off limits (inside a host callback or a driver-managed region
-// that forbids new allocations, real-time loops that must not hit the
-// allocator or its implicit synchronisation, or plugins whose host application
-// owns every device allocation).  The look-back state lives in this file-scope
+// For callers that cannot allocate device memory: a host thread that must
+// not enter the device allocator (a real-time loop that cannot afford its
+// latency or its implicit synchronisation), or a plugin whose host
+// application owns every device allocation and hands it only the arrays it
+// works on.  The look-back state lives in this file-scope
 // device array instead of a caller workspace.  Each GPU that loads the library
 // holds the array until the process exits.
 namespace edpp {

@@ -324,9 +324,9 @@ int edpp_stream_triad_i32(const int32_t *a, const int32_t *b, int32_t *c,
 
 /* Exclusive int32 look-back scan that allocates nothing and takes no
  * workspace.  It has no counterpart in the reference; it exists for callers
- * that cannot allocate device memory at the point of the call (host
- * callbacks, real-time loops that must not touch the allocator, plugins whose
- * host owns all device allocations).  Its scratch is one 1 MiB array in device
+ * that cannot allocate device memory at the point of the call (a host thread
+ * that must not enter the device allocator, such as a real-time loop, or a
+ * plugin whose host owns all device allocations).  Its scratch is one 1 MiB array in device
  * global memory that every GPU loading the library holds until exit, so
  * length is limited to edpp_scan_exclusive_i32_noalloc_max_length()
  * (536,739,840 elements); longer inputs return EDPP_EINVAL.  The first call on

@@ -11,9 +11,9 @@
                                (cuda/test_{split,gather,scatter,bandwidth}.cu)
                                compiled for sm_103a
 
-The oracle/_ref outputs are built only when the reference tree is present
-(EDPP_REFERENCE, default /root/reference).  Nothing here is part of the
-product.
+The oracle/_ref outputs are built only when the reference tree is present:
+EDPP_REFERENCE, or else a directory named `reference` beside this
+repository's root.  Nothing here is part of the product.
 """
 from __future__ import annotations
 
@@ -28,7 +28,7 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 REF_OUT = HERE / "_ref"
-REFERENCE = Path(os.environ.get("EDPP_REFERENCE", "/root/reference"))
+REFERENCE = Path(os.environ.get("EDPP_REFERENCE", str(HERE.parent.parent / "reference")))
 
 REF_CUDA_SOURCES = ["test_split", "test_gather", "test_scatter", "test_bandwidth"]
 

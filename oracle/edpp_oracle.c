@@ -548,3 +548,30 @@ uint64_t orc_join_count(const int32_t *r, int64_t r_len, const int32_t *s, int64
   free(b);
   return total;
 }
+
+/* ---- seeded inputs for the CPU side of the benchmark ----------------------
+ * Draw i of stream `seed` is splitmix64's output function (Steele, Lea, Flood,
+ * OOPSLA 2014) applied to seed + (i+1)*golden-gamma; a draw bounded to [0, r)
+ * is Lemire's multiply-shift on its high 32 bits.  The permutation is
+ * Durstenfeld's Fisher-Yates: for i = n-1 .. 1, swap a[i] with a[j],
+ * j = bounded(draw k, i+1), k = n-1-i.  The reference's own generator
+ * (random_generator_int_unique, openmp/util/utility.cpp:90-104) seeds from
+ * time() and is not reproducible, so both sides of a comparison are fed this
+ * one; it gives the same array as the library's data generator, which a CPU
+ * test checks. */
+static uint64_t orc_mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+void orc_gen_permutation_i32(int32_t *out, int64_t n, uint64_t seed) {
+  for (int64_t i = 0; i < n; ++i) out[i] = (int32_t)i;
+  for (int64_t i = n - 1; i > 0; --i) {
+    const uint64_t x = orc_mix64(seed + (uint64_t)(n - i) * 0x9E3779B97F4A7C15ull);
+    const int64_t j = (int64_t)(((x >> 32) * (uint64_t)(i + 1)) >> 32);
+    const int32_t t = out[i];
+    out[i] = out[j];
+    out[j] = t;
+  }
+}

@@ -84,6 +84,11 @@ double orc_average_hampel(const double *x, int n);
 
 int orc_max_threads(void);
 
+/* ---- seeded Fisher-Yates permutation of [0, n) (splitmix64 draws), the
+ *      benchmark's gather/scatter index array; replaces the reference's
+ *      time()-seeded random_generator_int_unique (openmp/util/utility.cpp:90-104) ---- */
+void orc_gen_permutation_i32(int32_t *out, int64_t n, uint64_t seed);
+
 #ifdef __cplusplus
 }
 #endif

@@ -40,6 +40,7 @@ _SIG = {
     "orc_compute_bandwidth": (_D, [ctypes.c_uint64, _I, _D]),
     "orc_average_hampel": (_D, [_VP, _I]),
     "orc_max_threads": (_I, []),
+    "orc_gen_permutation_i32": (None, [_VP, _I64, ctypes.c_uint64]),
 }
 
 _lib = None
@@ -210,6 +211,14 @@ def compute_bandwidth(num, word_size, ms):
 
 def max_threads():
     return lib().orc_max_threads()
+
+
+def gen_permutation(n, seed):
+    """Seeded Fisher-Yates permutation of [0, n): the same array as the
+    library's generator, made without loading the library."""
+    a = np.empty(n, np.int32)
+    lib().orc_gen_permutation_i32(_p(a), n, seed)
+    return a
 
 
 # ---- the reference itself -------------------------------------------------------

@@ -72,3 +72,35 @@ def test_inputs_deterministic(batch):
     assert np.array_equal(np.sort(idx), np.arange(g["length"], dtype=np.int32))
     sc = a0[:3000]
     assert sc.min() >= 0 and sc.max() <= 100
+
+
+def test_launch_rejects_missing_value_arrays(batch, edpp):
+    """Gather tiles read in1 and split tiles read in1 and write out1: a NULL
+    for either is an argument error, returned before any device work (the
+    pointers below are never dereferenced)."""
+    lib = edpp.lib()
+    fake = ctypes.c_void_p(256)
+    nul = ctypes.c_void_p(0)
+    for ops, need_in1, need_out1 in (([0], False, False), ([2], True, False),
+                                     ([1], True, True), ([0, 2, 1], True, True)):
+        segs = batch.layout([5000] * len(ops), ops)
+        plan = batch.Plan(segs)
+        wsb = plan.workspace_bytes
+        tu = batch.Tuning()
+        best_ms = ctypes.c_float()
+        sp = ctypes.c_void_p(segs.ctypes.data)
+        for in1, out1 in ((nul, fake), (fake, nul)):
+            expect_bad = (in1.value is None and need_in1) or (out1.value is None and need_out1)
+            if not expect_bad:
+                continue
+            assert lib.edpp_batch_launch(plan.h, fake, in1, fake, out1, fake, wsb,
+                                         nul) == edpp.EDPP_EINVAL
+            assert lib.edpp_batch_run_plain(sp, len(segs), fake, in1, fake, out1, fake, 1 << 30,
+                                            nul) == edpp.EDPP_EINVAL
+            assert lib.edpp_batch_autotune(sp, len(segs), fake, in1, fake, out1, fake, wsb, nul,
+                                           1, ctypes.byref(tu),
+                                           ctypes.byref(best_ms)) == edpp.EDPP_EINVAL
+    # scan-only batches need neither
+    segs = batch.layout([5000], [0])
+    assert lib.edpp_batch_run_plain(ctypes.c_void_p(segs.ctypes.data), 1, nul, nul, nul, nul,
+                                    fake, 1 << 30, nul) == edpp.EDPP_EINVAL  # in0/out0 missing

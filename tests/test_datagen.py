@@ -66,3 +66,10 @@ def test_uniform_keys_and_floats(edpp):
     assert f.min() >= -1.0 and f.max() < 1.0 and abs(f.mean()) < 0.02
     g = edpp.gen_uniform_i64(1000, 1, 0, 100)
     assert g.min() >= 0 and g.max() <= 100
+
+
+def test_oracle_permutation_equals_library_generator(edpp, orc):
+    """The reference arm of the benchmark makes its index array with the
+    oracle's generator (it must not load the library); it is the same array."""
+    for n, seed in ((0, 2), (1, 2), (2, 2), (1000, 2), (1 << 20, 2), ((1 << 20) + 7, 5)):
+        np.testing.assert_array_equal(orc.gen_permutation(n, seed), edpp.gen_permutation(n, seed))

@@ -115,3 +115,28 @@ def test_admission_waits_for_memory(cuda, edpp, serve):
     for i, s in enumerate(segs):
         o, L = int(s["offset"]), int(s["length"])
         np.testing.assert_array_equal(mix[i][0], e0[o:o + L])
+
+
+def test_batches_overlap_in_flight(cuda, edpp, serve):
+    """With one request per batch and four slots, requests submitted together
+    run as several batches on separate streams at once (their copies and
+    kernels can overlap on the device), and each result still equals the
+    oracle."""
+    sizes = [1 << 22] * 8
+    segs, in0, in1, reqs = _requests(edpp, serve, sizes, seed=23)
+    e0, e1 = reference_outputs(segs, in0, in1)
+    with serve.Server(pool_bytes=1 << 30, slots=4, max_batch_requests=1) as srv:
+        outs = [(serve.pinned_empty(len(a0)), serve.pinned_empty(len(a0))) for _, a0, _ in reqs]
+        ids = [srv.submit(op, a0, a1, o0, o1, buckets=64)
+               for (op, a0, a1), (o0, o1) in zip(reqs, outs)]
+        for rid in ids:
+            st, _ = srv.wait(rid)
+            assert st == 0
+        stats = srv.stats()
+    assert stats["batches"] == len(reqs)
+    assert stats["max_batches_in_flight"] > 1, stats
+    for i, s in enumerate(segs):
+        o, L, op = int(s["offset"]), int(s["length"]), int(s["op"])
+        np.testing.assert_array_equal(outs[i][0], e0[o:o + L])
+        if op == 1:
+            np.testing.assert_array_equal(outs[i][1], e1[o:o + L])

@@ -1,15 +1,19 @@
 """The allocation-free exclusive scan, edpp_scan_exclusive_i32_noalloc.
 
-Some callers cannot allocate device memory where they call the scan (inside
-a host callback, in a loop that must never touch the allocator, or as a
-plugin whose host application owns every device allocation).  This entry
-point keeps its look-back state in a fixed 1 MiB device array inside the
-library instead of a caller workspace.  The test calls it through the C ABI
-twice in a row, with different lengths so that the second call must clear
-what the first left in the shared array, and compares each result with the
+Some callers cannot allocate device memory where they call the scan: a host
+thread that must never enter the device allocator (a real-time loop that
+cannot afford its latency or implicit synchronisation), or a plugin whose
+host application owns every device allocation.  This entry point keeps its
+look-back state in a fixed 1 MiB device array inside the library instead of
+a caller workspace.
+
+The tests call it through the C ABI twice in a row, with different lengths
+so that the second call must clear what the first left in the shared array,
+and compare each result with the oracle's sequential scan and with the
 workspace-taking edpp_scan_exclusive_i32 (LOOKBACK) on the same input.
-Integer scans are compared exactly.  This file is named to be collected
-last.
+Integer scans are compared exactly.  A further test checks the defining
+property: after a warm-up call, calls at the maximum length leave the
+device's free memory unchanged.  This file is named to be collected last.
 """
 import ctypes
 
@@ -31,9 +35,10 @@ def _scan_with_workspace(edpp, torch, x):
     return out
 
 
-def _scan_noalloc(edpp, torch, x):
+def _scan_noalloc(edpp, torch, x, out=None):
     lib = edpp.lib()
-    out = torch.full_like(x, -1)
+    if out is None:
+        out = torch.full_like(x, -1)
     st = lib.edpp_scan_exclusive_i32_noalloc(ctypes.c_void_p(x.data_ptr()),
                                              ctypes.c_void_p(out.data_ptr()), x.numel(),
                                              edpp.current_stream_handle())
@@ -41,17 +46,45 @@ def _scan_noalloc(edpp, torch, x):
     return out
 
 
-def test_noalloc_matches_workspace_scan_twice(cuda, edpp):
+def test_noalloc_matches_oracle_and_workspace_scan_twice(cuda, edpp, orc):
     torch = cuda
     # first call: a long input (many tiles of look-back state); second call:
     # a shorter one that reuses the front of the same state.
     for n, seed, lo, hi in ((3_000_017, 1, 0, 15), (123_457, 2, 2**30, 2**31 - 1)):
-        x = torch.from_numpy(edpp.gen_uniform_i32(n, seed, lo, hi)).cuda()
+        h = edpp.gen_uniform_i32(n, seed, lo, hi)
+        x = torch.from_numpy(h).cuda()
         ref = _scan_with_workspace(edpp, torch, x)
         got = _scan_noalloc(edpp, torch, x)
         torch.cuda.synchronize()
         assert edpp.sync_status() == edpp.EDPP_OK
-        assert torch.equal(got, ref), f"mismatch at n={n}"
+        expect = orc.scan(h, False)
+        assert np.array_equal(got.cpu().numpy(), expect), f"differs from the oracle at n={n}"
+        assert torch.equal(got, ref), f"differs from the workspace scan at n={n}"
+
+
+def test_noalloc_leaves_free_memory_unchanged(cuda, edpp, orc):
+    torch = cuda
+    lib = edpp.lib()
+    n = lib.edpp_scan_exclusive_i32_noalloc_max_length()
+    h = edpp.gen_uniform_i32(n, 3, 0, 7)
+    x = torch.from_numpy(h).cuda()
+    out = torch.empty_like(x)
+    _scan_noalloc(edpp, torch, x, out)  # warm-up: module load, fault word, address lookup
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(3):
+        _scan_noalloc(edpp, torch, x, out)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert edpp.sync_status() == edpp.EDPP_OK
+    assert free1 == free0, f"free device memory changed by {free0 - free1} bytes"
+    # the full-length result, checked through its closed form on the device:
+    # consecutive differences give back the input, and the last element plus
+    # the last input is the wrapping total
+    assert torch.equal(out[1:] - out[:-1], x[:-1])
+    total = int(np.sum(h.astype(np.int64))) & 0xFFFFFFFF
+    last = (int(out[-1].item()) + int(h[-1])) & 0xFFFFFFFF
+    assert out[0].item() == 0 and last == total
 
 
 def test_noalloc_limit_and_arguments(cuda, edpp):
