@@ -7,6 +7,11 @@
   oracle/_ref/libref_omp.so    the reference's own OpenMP functions, compiled
                                from where they lie under the reference tree
                                with main() renamed, plus ref_shim.cpp
+  oracle/_ref/libref_cl_split_{ko,soa,aos}.so
+                               the reference's OpenCL split kernels
+                               (opencl/kernels/split_kernel.cl, included
+                               unchanged) compiled as C through ref_cl_shim.h,
+                               with ref_cl_runner.c replaying WI_split
   oracle/_ref/*.cubin          the reference's CUDA device code
                                (cuda/test_{split,gather,scatter,bandwidth}.cu)
                                compiled for sm_103a
@@ -94,6 +99,29 @@ def build_ref_omp() -> Path | None:
     return out
 
 
+CL_LAYOUTS = {"ko": "KO", "soa": "KVS_SOA", "aos": "KVS_AOS"}
+
+
+def build_ref_cl_split() -> list[Path]:
+    """The reference's OpenCL split kernels, compiled as C for the CPU: one
+    library per data layout (the -D flag the reference's host code gives its
+    kernel compiler, opencl/primitives/splitImpl.cpp:61-64).  Plain C with
+    pthreads, so it builds on any host where the reference tree exists."""
+    cl = REFERENCE / "opencl" / "kernels" / "split_kernel.cl"
+    if not cl.is_file():
+        return []
+    REF_OUT.mkdir(exist_ok=True)
+    shim, runner = HERE / "ref_cl_shim.h", HERE / "ref_cl_runner.c"
+    outs = []
+    for name, flag in CL_LAYOUTS.items():
+        out = REF_OUT / f"libref_cl_split_{name}.so"
+        if _newer(out, shim, runner, cl, REFERENCE / "opencl" / "params.h"):
+            _run(["gcc", "-O2", "-std=gnu11", "-w", "-pthread", "-fPIC", "-shared", f"-D{flag}",
+                  f'-DREF_SPLIT_CL="{cl}"', "-include", str(shim), str(runner), "-o", str(out)])
+        outs.append(out)
+    return outs
+
+
 def build_ref_cubins() -> list[Path]:
     """The reference's CUDA device code for sm_103a (GPU code: it travels to
     the GPU machine with the repository snapshot)."""
@@ -138,6 +166,12 @@ def build_all(verbose: bool = False) -> dict:
         res["ref_omp"] = build_ref_omp()
     except RuntimeError as e:  # the reference failing to build is reported, not fatal
         res["ref_omp"] = None
+        if verbose:
+            print(e, file=sys.stderr)
+    try:
+        res["ref_cl_split"] = build_ref_cl_split()
+    except RuntimeError as e:
+        res["ref_cl_split"] = []
         if verbose:
             print(e, file=sys.stderr)
     try:

@@ -6,6 +6,8 @@ leg of bench.py; never by the product.  Wraps:
   _ref/libref_omp.so     the reference's own OpenMP functions (x86, built
                          only where the reference tree is present)
   _build/libref_cuda.so  runner of the reference's CUDA kernels (cubins)
+  _ref/libref_cl_split_*.so  the reference's OpenCL WI_split kernels compiled
+                         as C (ref_cl_shim.h, ref_cl_runner.c)
 """
 from __future__ import annotations
 
@@ -245,6 +247,41 @@ def ref_omp():
         L.ref_compute_bandwidth.argtypes = [ctypes.c_uint64, _I, _D]
         _ref = L
     return _ref
+
+
+_refcl = {}
+
+
+def ref_cl_split(layout):
+    """The reference's own WI_split (its OpenCL kernels compiled as C), for
+    layout 'ko' | 'soa' | 'aos', or None where it was not built."""
+    if layout not in _refcl:
+        path = HERE / "_ref" / f"libref_cl_split_{layout}.so"
+        if not path.exists():
+            return None
+        L = ctypes.CDLL(str(path))
+        L.ref_wi_split.restype = _I
+        L.ref_wi_split.argtypes = [_VP, _VP, _I, _I, _I, _I, _VP, _VP]
+        _refcl[layout] = L
+    return _refcl[layout]
+
+
+def ref_wi_split(keys, buckets, values=None, aos=False, local_size=256, grid_size=32768):
+    """Run the reference's WI_split (KO, SOA with values, or AOS pairs);
+    returns (out, values_out) or None where it is not built."""
+    layout = "aos" if aos else ("soa" if values is not None else "ko")
+    L = ref_cl_split(layout)
+    if L is None:
+        return None
+    keys = _c(keys, np.int32)
+    out = np.zeros_like(keys)
+    vals = _c(values, np.int32) if layout == "soa" else None
+    vo = np.zeros_like(vals) if vals is not None else None
+    rc = L.ref_wi_split(_p(keys), _p(vals), keys.shape[0], buckets, local_size, grid_size, _p(out),
+                        _p(vo))
+    if rc != 0:
+        raise ValueError("the reference cannot run this WI_split configuration")
+    return out, vo
 
 
 _refcu = None

@@ -8,6 +8,12 @@ the reference tree into oracle/_ref/libref_omp.so by oracle/build.py, on
 seeded inputs from the package's generators.  Run here, where the reference
 tree exists:   python tests/golden/make_golden.py
 
+reference_cl_wi_split.npz (written by --cl, where the reference tree exists):
+outputs of the reference's own WI_split (WI_histogram, exclusive scan,
+WI_shuffle of opencl/kernels/split_kernel.cl, compiled as C by
+oracle/build.py through oracle/ref_cl_shim.h) for KO, KVS_SOA and KVS_AOS on
+several work-group shapes.
+
 reference_cuda.npz (written by --cuda, on a GPU machine): outputs of the
 reference's CUDA split (pre_scan / ExclusiveSum / post_scan), gather_kernel,
 scatter_kernel and int32 STREAM kernels, launched from the reference's
@@ -104,8 +110,43 @@ def make_cuda(out_path: Path):
     print(f"wrote {out_path} ({out_path.stat().st_size} bytes, {len(g)} arrays)")
 
 
+# (n, local_size, grid_size, buckets) of the WI_split fixtures: work-group
+# shapes from one work-item per group to 256, grids from 3 to 128 groups,
+# inputs shorter than the work-item count, 2 to 1024 buckets
+WI_CASES = [(8191, 32, 16, 64), (6007, 64, 7, 2), (5000, 16, 3, 1024), (8191, 256, 8, 256),
+            (4099, 256, 128, 16), (3001, 1, 39, 8)]
+
+
+def make_cl(out_path: Path):
+    orc.build()
+    g = {}
+    for c, (n, local, grid, B) in enumerate(WI_CASES):
+        keys = edpp.gen_keys_uniform(n, 30 + c)
+        vals = np.arange(n, dtype=np.int32)
+        ko = orc.ref_wi_split(keys, B, local_size=local, grid_size=grid)
+        so = orc.ref_wi_split(keys, B, vals, local_size=local, grid_size=grid)
+        ao = orc.ref_wi_split(np.stack([keys, vals], axis=1), B, aos=True, local_size=local,
+                              grid_size=grid)
+        if ko is None or so is None or ao is None:
+            raise SystemExit("reference OpenCL split not built (needs the reference tree)")
+        # The order does not depend on the layout: the SOA values (input
+        # index) are the permutation, and every layout's output is the keys
+        # (and indices) in that order.  Only the permutation is stored; the
+        # keys are regenerated from their seed (generator checked by sum).
+        perm = so[1]
+        assert np.array_equal(ko[0], keys[perm]) and np.array_equal(so[0], keys[perm])
+        assert np.array_equal(ao[0], np.stack([keys[perm], perm], axis=1))
+        g[f"wi{c}_params"] = np.array([n, local, grid, B, 30 + c,
+                                       int(keys.astype(np.int64).sum())], np.int64)
+        g[f"wi{c}_perm"] = perm
+    np.savez_compressed(out_path, **g)
+    print(f"wrote {out_path} ({out_path.stat().st_size} bytes, {len(g)} arrays)")
+
+
 if __name__ == "__main__":
-    if "--cuda" in sys.argv:
+    if "--cl" in sys.argv:
+        make_cl(HERE / "reference_cl_wi_split.npz")
+    elif "--cuda" in sys.argv:
         dst = Path(sys.argv[sys.argv.index("--cuda") + 1]) if len(sys.argv) > 2 else \
             HERE / "reference_cuda.npz"
         make_cuda(dst)

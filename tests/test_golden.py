@@ -6,6 +6,8 @@ reference_omp.npz   the reference's OpenMP functions (gather, scatter,
 reference_cuda.npz  the reference's CUDA kernels (warp-ballot split,
                     gather_kernel, scatter_kernel, int32 STREAM) and the CUB
                     ExclusiveSum call of its scan test
+reference_cl_wi_split.npz  the reference's OpenCL WI_split (WI_histogram /
+                    WI_shuffle compiled as C), as the permutation it applies
 
 The oracle must reproduce every vector (CPU tests); the GPU primitives must
 too (gpu tests).
@@ -25,6 +27,34 @@ def load(name):
     if not p.exists():
         pytest.skip(f"{name} not generated")
     return dict(np.load(p))
+
+
+def wi_cases(edpp):
+    """(n, local, grid, buckets, keys, perm) of every WI_split fixture; the
+    keys are regenerated from their seed and checked against the stored sum."""
+    g = load("reference_cl_wi_split.npz")
+    out = []
+    for c in range(len([k for k in g if k.endswith("_params")])):
+        n, local, grid, B, seed, ksum = (int(v) for v in g[f"wi{c}_params"])
+        keys = edpp.gen_keys_uniform(n, seed)
+        assert int(keys.astype(np.int64).sum()) == ksum
+        out.append((n, local, grid, B, keys, g[f"wi{c}_perm"]))
+    return out
+
+
+def test_oracle_wi_split_vectors(orc, edpp):
+    """The restated WI_split order equals the reference's own kernels' output
+    in every layout."""
+    for n, local, grid, B, keys, perm in wi_cases(edpp):
+        vals = np.arange(n, dtype=np.int32)
+        ko, _ = orc.split_wi(keys, B, local_size=local, grid_size=grid)
+        np.testing.assert_array_equal(ko, keys[perm])
+        sk, sv = orc.split_wi(keys, B, vals, local_size=local, grid_size=grid)
+        np.testing.assert_array_equal(sk, keys[perm])
+        np.testing.assert_array_equal(sv, perm)
+        ak, _ = orc.split_wi(np.stack([keys, vals], axis=1), B, aos=True, local_size=local,
+                             grid_size=grid)
+        np.testing.assert_array_equal(ak, np.stack([keys[perm], perm], axis=1))
 
 
 # ---- oracle against the reference's vectors ----------------------------------

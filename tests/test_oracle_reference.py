@@ -84,3 +84,26 @@ def test_compute_bandwidth_matches_reference(orc, ref):
     for num, w, ms in ((1 << 28, 4, 3.5), (12345, 8, 0.25)):
         assert orc.compute_bandwidth(num, w, ms) == pytest.approx(
             ref.ref_compute_bandwidth(num, w, ms), rel=1e-15)
+
+
+@pytest.mark.parametrize("n,local,grid,B", [(1, 32, 2, 4), (100003, 32, 16, 64), (77777, 64, 7, 2),
+                                            (5000, 16, 3, 1024), (65536, 128, 64, 256),
+                                            (999, 1, 39, 16)])
+def test_wi_split_restatement_matches_reference_kernels(orc, edpp, n, local, grid, B):
+    """The reference's own OpenCL WI_split, compiled as C (oracle/_ref), on
+    the same seeded keys as the restatement, every layout."""
+    if orc.ref_cl_split("ko") is None:
+        pytest.skip("reference OpenCL split not built on this host")
+    keys = edpp.gen_keys_uniform(n, 11)
+    vals = np.arange(n, dtype=np.int32)
+    rk, _ = orc.ref_wi_split(keys, B, local_size=local, grid_size=grid)
+    ek, _ = orc.split_wi(keys, B, local_size=local, grid_size=grid)
+    np.testing.assert_array_equal(rk, ek)
+    rk, rv = orc.ref_wi_split(keys, B, vals, local_size=local, grid_size=grid)
+    ek, ev = orc.split_wi(keys, B, vals, local_size=local, grid_size=grid)
+    np.testing.assert_array_equal(rk, ek)
+    np.testing.assert_array_equal(rv, ev)
+    pairs = np.stack([keys, vals], axis=1)
+    ra, _ = orc.ref_wi_split(pairs, B, aos=True, local_size=local, grid_size=grid)
+    ea, _ = orc.split_wi(pairs, B, aos=True, local_size=local, grid_size=grid)
+    np.testing.assert_array_equal(ra, ea)

@@ -126,3 +126,23 @@ def test_wi_split_order(cuda, edpp, orc, layout, n, local, grid, B):
         np.testing.assert_array_equal(to_host(ko), ek)
         if v is not None:
             np.testing.assert_array_equal(to_host(vo), ev)
+
+
+@pytest.mark.parametrize("layout", ["ko", "soa", "aos"])
+def test_wi_split_matches_reference_kernel_vectors(cuda, edpp, layout):
+    """edpp_split_i32_wi against the output of the reference's own OpenCL
+    WI_split kernels (tests/golden/reference_cl_wi_split.npz)."""
+    from test_golden import wi_cases
+    for n, local, grid, B, keys, perm in wi_cases(edpp):
+        vals = np.arange(n, dtype=np.int32)
+        if layout == "aos":
+            ko, _ = edpp.split_wi(to_dev(np.stack([keys, vals], axis=1)), B, layout="aos",
+                                  local_size=local, grid_size=grid)
+            np.testing.assert_array_equal(to_host(ko), np.stack([keys[perm], perm], axis=1))
+        else:
+            v = vals if layout == "soa" else None
+            ko, vo = edpp.split_wi(to_dev(keys), B, None if v is None else to_dev(v),
+                                   layout=layout, local_size=local, grid_size=grid)
+            np.testing.assert_array_equal(to_host(ko), keys[perm])
+            if v is not None:
+                np.testing.assert_array_equal(to_host(vo), perm)
