@@ -200,18 +200,19 @@ template <typename T> __global__ void __launch_bounds__(1024) scan_partials_kern
 // Scan tiles [t_lo, t_hi) in order starting from `running`; returns the
 // running sum after the last tile (false: a bulk copy timed out).  `bar`
 // must be initialised; buffers and barriers are the caller's shared memory.
+// `phase` (bit s: parity of bar[s]'s next completion) carries over between
+// calls on the same barriers.
 template <typename T, bool kInclusive, bool kStreamOut = false>
 __device__ bool scan_tile_run(const T *in, T *out, int64_t n, int64_t t_lo, int64_t t_hi,
                               T &running, T (*buf)[TS<T>::kTile], typename TS<T>::Shared &sh,
-                              uint64_t *bar, bool tma, bool vec_out, uint64_t timeout_ns,
-                              unsigned *fault) {
+                              uint64_t *bar, uint32_t &phase, bool tma, bool vec_out,
+                              uint64_t timeout_ns, unsigned *fault) {
   using S = TS<T>;
   constexpr int kTile = S::kTile;
   auto count_of = [&](int64_t t) { return static_cast<int>(min64(kTile, n - t * kTile)); };
   // Prologue: stage the first tile.
   uint32_t bulk_cur = stage_tile<T, kTile, kThreads>(buf[0], in + t_lo * kTile, count_of(t_lo), tma,
                                                      &bar[0]);
-  uint32_t phase = 0;  // bit s: parity of the next completion of bar[s]
   for (int64_t t = t_lo; t < t_hi; ++t) {
     const int slot = static_cast<int>((t - t_lo) & 1);
     const int count = count_of(t);
@@ -263,9 +264,10 @@ __global__ void __launch_bounds__(kThreads)
   }
   __syncthreads();
   T running = kFromOffsets ? offsets[blockIdx.x] : zero_of<T>();
+  uint32_t phase = 0;
   if (t_lo < t_hi &&
-      !scan_tile_run<T, kInclusive>(in, out, n, t_lo, t_hi, running, buf, sh, bar, tma, vec_out,
-                                    timeout_ns, fault))
+      !scan_tile_run<T, kInclusive>(in, out, n, t_lo, t_hi, running, buf, sh, bar, phase, tma,
+                                    vec_out, timeout_ns, fault))
     return;
   if (!kFromOffsets && threadIdx.x == 0) totals[blockIdx.x] = running;
 }
@@ -339,9 +341,137 @@ __global__ void __launch_bounds__(kThreads)
   for (int k = 0; k < kThreads / 32; ++k) running = op_add(running, s_pre[k]);
   // 4. scan the tiles again from L2; the output streams out (evict-first),
   // so it does not push the input's remaining lines out of L2
+  uint32_t phase = 0;
   if (t_lo < t_hi)
-    scan_tile_run<T, kInclusive, true>(in, out, n, t_lo, t_hi, running, buf, sh, bar, tma,
+    scan_tile_run<T, kInclusive, true>(in, out, n, t_lo, t_hi, running, buf, sh, bar, phase, tma,
                                        vec_out, timeout_ns, fault);
+}
+
+// Reduce-then-scan for inputs larger than L2, in one cooperative launch.  A
+// persistent grid of G blocks walks the input in chunks of G slices of
+// kSliceTiles tiles; block b owns slice b of every chunk.  In iteration c a
+// block first reduces its slice of chunk c+1 (read from DRAM with the normal
+// L2 policy, so its lines stay in L2) and publishes the sum, then waits until
+// all G sums of chunk c are published (they were, one iteration earlier,
+// unless some block lags by a whole iteration), adds up the sums of the
+// slices before its own and the chunk total, and scans its slice of chunk c
+// again, from L2, streaming the output (evict-first, so it does not push the
+// next chunk's lines out).  DRAM traffic is 8 bytes per int32 element, as for
+// the look-back scan, with no chain of tile-to-tile waits: the only wait is
+// one count per chunk, a whole iteration after it started filling.  Waits are
+// bounded; a block that gives up raises EDPP_FAULT_TIMEOUT and sets the
+// call's abort flag so the others stop too.
+constexpr int kSliceTiles = 2;
+
+template <typename T, bool kInclusive>
+__global__ void __launch_bounds__(kThreads, 4)
+    rts_chunked_kernel(const T *in, T *out, int64_t n, int64_t chunks, T *sums, unsigned *cnt,
+                       unsigned *abort_flag, bool tma, bool vec_out, uint64_t timeout_ns,
+                       unsigned *fault) {
+  using S = TS<T>;
+  constexpr int kTile = S::kTile;
+  __shared__ alignas(128) T buf[2][kTile];
+  __shared__ typename S::Shared sh;
+  __shared__ alignas(8) uint64_t bar[2];
+  __shared__ T s_red[2][kThreads / 32];
+  __shared__ int s_ok;
+  const int64_t G = gridDim.x, b = blockIdx.x;
+  const int64_t num_tiles = (n + kTile - 1) / kTile;
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  auto reduce_publish = [&](int64_t c) {
+    const int64_t lo = min64(n, (c * G + b) * kSliceTiles * kTile);
+    const int64_t hi = min64(n, lo + kSliceTiles * kTile);
+    T v;
+    if (tma && hi - lo == kSliceTiles * kTile) {
+      // a whole slice: every 16-byte load of the slice in flight at once
+      constexpr int kV = kSliceTiles * kChunks;
+      constexpr int E = Chunk<T>::E;
+      const uint4 *p = reinterpret_cast<const uint4 *>(in + lo);
+      Chunk<T> q[kV];
+#pragma unroll
+      for (int k = 0; k < kV; ++k) q[k].raw = __ldcg(p + k * kThreads + tid);
+      T acc = zero_of<T>();
+#pragma unroll
+      for (int k = 0; k < kV; ++k)
+#pragma unroll
+        for (int e = 0; e < E; ++e) acc = op_add(acc, q[k].e[e]);
+      acc = warp_sum(acc);
+      if ((tid & 31) == 0) s_red[0][tid >> 5] = acc;
+      __syncthreads();
+      v = zero_of<T>();
+      if (tid == 0) {
+#pragma unroll
+        for (int k = 0; k < kThreads / 32; ++k) v = op_add(v, s_red[0][k]);
+      }
+      __syncthreads();  // s_red is reused below
+    } else {
+      v = block_reduce_range<T, true>(in, lo, hi, tma);  // valid in thread 0
+    }
+    if (tid == 0) {
+      sums[c * G + b] = v;
+      __threadfence();  // the sum is visible before the count that announces it
+      atomicAdd(&cnt[c], 1u);
+    }
+  };
+  reduce_publish(0);
+  T base = zero_of<T>();
+  uint32_t phase = 0;
+  for (int64_t c = 0; c < chunks; ++c) {
+    if (c + 1 < chunks) reduce_publish(c + 1);
+    if (tid == 0) {
+      const uint32_t need = static_cast<uint32_t>(G);
+      bool ok = ld_acquire_u32(&cnt[c]) >= need;
+      if (!ok) {
+        const uint64_t t0 = globaltimer_ns();
+        while (!(ok = ld_acquire_u32(&cnt[c]) >= need)) {
+          if (globaltimer_ns() - t0 > timeout_ns || fault_raised(abort_flag)) break;
+          __nanosleep(128);
+        }
+      }
+      if (!ok) {
+        raise_fault(fault, EDPP_FAULT_TIMEOUT);
+        atomicOr(abort_flag, 1u);
+      }
+      s_ok = ok ? 1 : 0;
+    }
+    __syncthreads();
+    if (!s_ok) return;
+    // sums of the slices before this block's, and the chunk total
+    T pre = zero_of<T>(), tot = zero_of<T>();
+    for (int64_t i = tid; i < G; i += kThreads) {
+      const T v = __ldcg(sums + c * G + i);
+      tot = op_add(tot, v);
+      if (i < b) pre = op_add(pre, v);
+    }
+    pre = warp_sum(pre);
+    tot = warp_sum(tot);
+    if ((tid & 31) == 0) {
+      s_red[0][tid >> 5] = pre;
+      s_red[1][tid >> 5] = tot;
+    }
+    __syncthreads();
+    pre = zero_of<T>();
+    tot = zero_of<T>();
+#pragma unroll
+    for (int k = 0; k < kThreads / 32; ++k) {
+      pre = op_add(pre, s_red[0][k]);
+      tot = op_add(tot, s_red[1][k]);
+    }
+    const int64_t t_lo = (c * G + b) * kSliceTiles;
+    const int64_t t_hi = min64(num_tiles, t_lo + kSliceTiles);
+    T running = op_add(base, pre);
+    if (t_lo < t_hi &&
+        !scan_tile_run<T, kInclusive, true>(in, out, n, t_lo, t_hi, running, buf, sh, bar, phase,
+                                            tma, vec_out, timeout_ns, fault))
+      return;
+    base = op_add(base, tot);
+    __syncthreads();  // s_red is rewritten in the next iteration
+  }
 }
 
 // SSA third pass: out[range of block b] += offsets[b].
@@ -387,10 +517,23 @@ template <typename T> int64_t tiles_of(int64_t n) {
   return (n + TS<T>::kTile - 1) / TS<T>::kTile;
 }
 
+// The chunked RTS: chunks * G slice sums (chunks * G <= slices + G) and one
+// count per chunk (chunks <= slices), after the header.
+template <typename T> int64_t slices_of(int64_t n) {
+  return (tiles_of<T>(n) + kSliceTiles - 1) / kSliceTiles;
+}
+template <typename T> size_t chunked_sums_bytes(int64_t n) {
+  return round_up(static_cast<size_t>(slices_of<T>(n) + kMaxChunkBlocks) * sizeof(T), 256);
+}
+
 template <typename T> size_t workspace_bytes(int64_t n, int algo) {
   if (n <= 0) return 0;
   if (algo == EDPP_SCAN_LOOKBACK) return kHeader + LookbackState<T>::bytes(tiles_of<T>(n));
-  return kHeader + round_up(static_cast<size_t>(kMaxChunkBlocks) * sizeof(T), 256);
+  const size_t three = kHeader + round_up(static_cast<size_t>(kMaxChunkBlocks) * sizeof(T), 256);
+  if (algo != EDPP_SCAN_RTS) return three;
+  const size_t chunked = kHeader + chunked_sums_bytes<T>(n) +
+                         round_up(static_cast<size_t>(slices_of<T>(n)) * 4, 256);
+  return std::max(three, chunked);
 }
 
 // Blocks of the RTS / SSA schemes: a few waves of resident blocks, each
@@ -474,6 +617,41 @@ int scan_impl(const T *in, T *out, int64_t n, int algo, void *ws, size_t ws_byte
     }
   }
   if (algo == EDPP_SCAN_RTS) {
+    // larger than L2: the chunked one-launch form, which reads each element
+    // from DRAM once
+    static int cresident[64];
+    static std::once_flag conce[64];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) dev = 0;
+    std::call_once(conce[dev], [dev] {
+      int per_sm = 0;
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+              &per_sm, rts_chunked_kernel<T, kInclusive>, kThreads, 0) != cudaSuccess)
+        per_sm = 0;
+      cresident[dev] = per_sm * device_sm_count();
+    });
+    if (cresident[dev] > 0) {
+      const int64_t slices = slices_of<T>(n);
+      const int64_t g = std::min<int64_t>({slices, cresident[dev], kMaxChunkBlocks});
+      const int64_t chunks = (slices + g - 1) / g;
+      T *sums = reinterpret_cast<T *>(w + kHeader);
+      unsigned *cnt = reinterpret_cast<unsigned *>(w + kHeader + chunked_sums_bytes<T>(n));
+      if (cudaMemsetAsync(w, 0, kHeader, st) != cudaSuccess ||
+          cudaMemsetAsync(cnt, 0, sizeof(unsigned) * static_cast<size_t>(chunks), st) !=
+              cudaSuccess)
+        return EDPP_ECUDA;
+      unsigned *abort_flag = reinterpret_cast<unsigned *>(w + 8);
+      int64_t n_arg = n, chunks_arg = chunks;
+      bool tma_arg = tma, vec_arg = vec_out;
+      uint64_t to_arg = timeout_ns;
+      void *args[] = {const_cast<T **>(&in), &out, &n_arg, &chunks_arg, &sums, &cnt, &abort_flag,
+                      &tma_arg, &vec_arg, &to_arg, &fault};
+      cudaLaunchCooperativeKernel(
+          reinterpret_cast<const void *>(rts_chunked_kernel<T, kInclusive>),
+          dim3(static_cast<unsigned>(g)), dim3(kThreads), args, 0, st);
+      return launch_status();
+    }
     reduce_blocks_kernel<T><<<static_cast<unsigned>(blocks), kThreads, 0, st>>>(in, n, per,
                                                                                 partials, tma);
     scan_partials_kernel<T><<<1, 1024, 0, st>>>(partials, static_cast<int>(blocks));

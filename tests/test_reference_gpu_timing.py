@@ -53,16 +53,19 @@ def test_reference_kernels_timed_beside_ours(cuda, edpp, orc):
                      "ours_ms": round(ours, 4), "ours_tiled_ms": round(tiled, 4)})
     del d_loc, d_in, out, ws
 
-    # exclusive int32 scan: CUB DeviceScan vs look-back, 2^28
+    # exclusive int32 scan: CUB DeviceScan vs look-back and vs the chunked
+    # reduce-then-scan (second read from L2), 2^28
     n = 1 << 28
     x = cuda.zeros(n, dtype=cuda.int32, device="cuda")
     y = cuda.empty_like(x)
-    sws = edpp.workspace(edpp.scan_workspace_bytes(n, "int32", "lookback"))
     assert rc.refcu_time_cub_scan(n, 10, ctypes.byref(ms)) == 0
-    ours = _ours_ms(cuda, lambda: edpp.scan(x, algo="lookback", out=y, ws=sws))
-    rows.append({"call": "exclusive scan int32 2^28 (CUB)", "reference_ms": round(ms.value, 4),
-                 "ours_ms": round(ours, 4)})
-    del x, y, sws
+    for algo in ("lookback", "rts"):
+        sws = edpp.workspace(edpp.scan_workspace_bytes(n, "int32", algo))
+        ours = _ours_ms(cuda, lambda: edpp.scan(x, algo=algo, out=y, ws=sws))
+        rows.append({"call": f"exclusive scan int32 2^28 (CUB) vs {algo}",
+                     "reference_ms": round(ms.value, 4), "ours_ms": round(ours, 4)})
+        del sws
+    del x, y
 
     # stable key-only split, 256 buckets, 2^24 keys < 256 (the reference's limits)
     n = 1 << 24
