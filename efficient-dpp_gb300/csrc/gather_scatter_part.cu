@@ -822,7 +822,10 @@ __global__ void __launch_bounds__(1024)
 }
 
 // Append every pair of one tile to fine window (pair.x >> fine_log) at that
-// window's cursor.  The tiles ("slots") are either the flat range [0, *total)
+// window's cursor, as two arrays: the offset of pair.x inside its window
+// (16 bits: windows are at most 2^15 elements) and pair.y.  Six bytes per
+// pair instead of eight, on the write here and on the read of every later
+// stage.  The tiles ("slots") are either the flat range [0, *total)
 // cut into kTile pairs, or, with region_log > 0, each region
 // [r << region_log, region_end[r]) cut the same way (slots past a region's
 // end are empty).  Either way the pairs are ordered by coarse window
@@ -865,7 +868,8 @@ __global__ void __launch_bounds__(kThreads, kRefineBlocksPerSm)
     win_refine_kernel(const int2 *__restrict__ src, const uint32_t *__restrict__ total_p,
                       const uint32_t *__restrict__ region_end, int region_log, int fine_log,
                       int coarse_log, int64_t slots, uint32_t *__restrict__ fill,
-                      int2 *__restrict__ dst, uint64_t timeout_ns, unsigned *fault) {
+                      uint16_t *__restrict__ dst_off, int32_t *__restrict__ dst_val,
+                      uint64_t timeout_ns, unsigned *fault) {
   extern __shared__ __align__(16) unsigned char smem[];
   int2 *bufs = reinterpret_cast<int2 *>(smem);  // [2][kTile]
   uint32_t *scnt = reinterpret_cast<uint32_t *>(bufs + 2 * kTile);
@@ -876,6 +880,7 @@ __global__ void __launch_bounds__(kThreads, kRefineBlocksPerSm)
   const int t = threadIdx.x;
   const int64_t G = gridDim.x;
   const int fan = coarse_log - fine_log;
+  const uint32_t wmask = (1u << fine_log) - 1u;
   for (int i = t; i < kRefineSpan; i += kThreads) scnt[i] = 0;
   if (t == 0) {
     s_total = 0;
@@ -948,7 +953,11 @@ __global__ void __launch_bounds__(kThreads, kRefineBlocksPerSm)
       if (!grouped) {  // skewed slot: one cursor claim per pair
 #pragma unroll
         for (int e = 0; e < kPer; ++e)
-          if (fid[e] >= 0) dst[atomicAdd(&fill[wlo + fid[e]], 1u)] = pr[e];
+          if (fid[e] >= 0) {
+            const uint32_t idx = atomicAdd(&fill[wlo + fid[e]], 1u);
+            dst_off[idx] = static_cast<uint16_t>(static_cast<uint32_t>(pr[e].x) & wmask);
+            dst_val[idx] = pr[e].y;
+          }
       } else {
         uint32_t g[kRefineSpan / kThreads], o[kRefineSpan / kThreads];
         claim_runs<kRefineSpan / kThreads, kThreads>(scnt, soff, span, fill + wlo, &s_total, g, o);
@@ -962,7 +971,9 @@ __global__ void __launch_bounds__(kThreads, kRefineBlocksPerSm)
         if (t == 0) s_total = 0;
         for (uint32_t q = t; q < total; q += kThreads) {
           const int2 p = buf[q];
-          dst[sgb[(p.x >> fine_log) - wlo] + q] = p;
+          const uint32_t idx = sgb[(p.x >> fine_log) - wlo] + q;
+          dst_off[idx] = static_cast<uint16_t>(static_cast<uint32_t>(p.x) & wmask);
+          dst_val[idx] = p.y;
         }
       }
       fence_proxy_async_smem();  // generic accesses of buf before the next bulk copy into it
@@ -990,16 +1001,17 @@ __global__ void __launch_bounds__(kThreads, kRefineBlocksPerSm)
 }
 
 // One block per fine window f: pairs [start[f], start[f+1]) (or, without
-// start, [f << fine_log, fill_end[f])) are {index, value} with index inside
-// the window; they are applied in shared memory and the written elements of
+// start, [f << fine_log, fill_end[f])) are {offset in the window, value}
+// (two arrays, as the refine writes them); they are applied in shared memory and the written elements of
 // the window are stored (a bitmap marks them; untouched elements keep their
 // old value in `out`).  unique: no index repeats (a gather's return trip),
 // so a window with as many pairs as elements is written whole and needs no
 // bitmap.
 __global__ void __launch_bounds__(kWinThreads)
-    win_apply_kernel(const int2 *__restrict__ pairs, const uint32_t *__restrict__ start,
-                     const uint32_t *__restrict__ fill_end, int fine_log, int64_t n,
-                     int32_t *__restrict__ out, bool vec_out, bool unique) {
+    win_apply_kernel(const uint16_t *__restrict__ poff, const int32_t *__restrict__ pval,
+                     const uint32_t *__restrict__ start, const uint32_t *__restrict__ fill_end,
+                     int fine_log, int64_t n, int32_t *__restrict__ out, bool vec_out,
+                     bool unique) {
   extern __shared__ __align__(16) int32_t win[];
   const int W = 1 << fine_log;
   uint32_t *bits = reinterpret_cast<uint32_t *>(win + W);
@@ -1013,32 +1025,42 @@ __global__ void __launch_bounds__(kWinThreads)
   if (!whole)
     for (int i = t; i < (W >> 5); i += kWinThreads) bits[i] = 0u;
   __syncthreads();
-  auto put = [&](int2 p) {
-    const int rel = static_cast<int>(p.x - base);
-    win[rel] = p.y;
+  auto put = [&](uint32_t rel, int32_t v) {
+    win[rel] = v;
     if (!whole) atomicOr(&bits[rel >> 5], 1u << (rel & 31));
   };
-  // pairs: scalar head to an even index, then two per 16-byte load
-  int64_t j = lo;
-  if ((j & 1) && j < hi) {
-    if (t == 0) put(pairs[j]);
-    ++j;
-  }
-  const int64_t nv = (hi - j) >> 1;
-  const int4 *p4 = reinterpret_cast<const int4 *>(pairs + j);
-  for (int64_t v = t; v < nv; v += 4 * kWinThreads) {
-    int4 q[4];
+  // pairs: a scalar head up to a multiple of 8, then groups of 8 (one 16-byte
+  // load of offsets, two of values; both arrays are 16-byte aligned), then a
+  // scalar tail
+  const int64_t head = min64(hi, (lo + 7) & ~int64_t{7});
+  for (int64_t q = lo + t; q < head; q += kWinThreads) put(poff[q], pval[q]);
+  const int64_t ng = (hi - head) >> 3;
+  const uint4 *o4 = reinterpret_cast<const uint4 *>(poff + head);
+  const uint4 *v4 = reinterpret_cast<const uint4 *>(pval + head);
+  for (int64_t g = t; g < ng; g += 2 * kWinThreads) {
+    uint4 qo[2], qv[4];
 #pragma unroll
-    for (int u = 0; u < 4; ++u)
-      if (v + u * kWinThreads < nv) q[u] = __ldcs(p4 + v + u * kWinThreads);
+    for (int u = 0; u < 2; ++u)
+      if (g + u * kWinThreads < ng) {
+        qo[u] = __ldcs(o4 + g + u * kWinThreads);
+        qv[2 * u] = __ldcs(v4 + 2 * (g + u * kWinThreads));
+        qv[2 * u + 1] = __ldcs(v4 + 2 * (g + u * kWinThreads) + 1);
+      }
 #pragma unroll
-    for (int u = 0; u < 4; ++u)
-      if (v + u * kWinThreads < nv) {
-        put(make_int2(q[u].x, q[u].y));
-        put(make_int2(q[u].z, q[u].w));
+    for (int u = 0; u < 2; ++u)
+      if (g + u * kWinThreads < ng) {
+        const uint32_t os[4] = {qo[u].x, qo[u].y, qo[u].z, qo[u].w};
+        const uint32_t vs[8] = {qv[2 * u].x, qv[2 * u].y, qv[2 * u].z, qv[2 * u].w,
+                                qv[2 * u + 1].x, qv[2 * u + 1].y, qv[2 * u + 1].z,
+                                qv[2 * u + 1].w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          put(os[k] & 0xffffu, static_cast<int32_t>(vs[2 * k]));
+          put(os[k] >> 16, static_cast<int32_t>(vs[2 * k + 1]));
+        }
       }
   }
-  if (t == 0 && j + 2 * nv < hi) put(pairs[j + 2 * nv]);
+  for (int64_t q = head + 8 * ng + t; q < hi; q += kWinThreads) put(poff[q], pval[q]);
   __syncthreads();
   for (int e0 = 4 * t; e0 < len; e0 += 4 * kWinThreads) {
     const uint32_t nib = whole ? 0xFu : (bits[e0 >> 5] >> (e0 & 31)) & 0xFu;
@@ -1053,7 +1075,8 @@ __global__ void __launch_bounds__(kWinThreads)
 }
 
 // Gather fetch: one block per fine window f of in[]; the window is loaded
-// once into shared memory, and each pair {loc, i} of the window becomes
+// once into shared memory, and each pair {loc, i} of the window (the offset
+// of loc in the window and i, in two arrays) becomes
 // {i, in[loc]}, appended to the coarse window of i (cursors cfill2).  The
 // window's pairs go in sub-tiles of kTile; each sub-tile's pairs are loaded
 // into registers while the previous one is grouped (the first while the
@@ -1062,7 +1085,8 @@ constexpr int kFetchThreads = 512;
 constexpr int kFetchPer = kTile / kFetchThreads;  // 8 pairs per thread per sub-tile
 
 __global__ void __launch_bounds__(kFetchThreads)
-    win_fetch_kernel(const int2 *__restrict__ pairs, const uint32_t *__restrict__ start,
+    win_fetch_kernel(const uint16_t *__restrict__ poff, const int32_t *__restrict__ pidx,
+                     const uint32_t *__restrict__ start,
                      const int32_t *__restrict__ in, int64_t n, int fine_log, int coarse_log,
                      int C, uint32_t *__restrict__ cfill2, int2 *__restrict__ dst, bool vec_in,
                      uint64_t timeout_ns, unsigned *fault) {
@@ -1080,12 +1104,14 @@ __global__ void __launch_bounds__(kFetchThreads)
   const int len = static_cast<int>(min64(W, n - base));
   const int64_t lo = start[f], hi = start[f + 1];
   if (lo >= hi) return;  // block-uniform
-  int2 nxt[kFetchPer];
+  uint32_t nxt_off[kFetchPer];
+  int32_t nxt_i[kFetchPer];
   auto load = [&](int64_t c0) {
 #pragma unroll
     for (int e = 0; e < kFetchPer; ++e) {
       const int64_t j = c0 + static_cast<int64_t>(e) * kFetchThreads + t;
-      nxt[e] = j < hi ? __ldcs(pairs + j) : make_int2(0, 0);
+      nxt_off[e] = j < hi ? __ldcs(poff + j) : 0u;
+      nxt_i[e] = j < hi ? __ldcs(pidx + j) : 0;
     }
   };
   // the window by one bulk copy (16-byte multiple), the rest by plain loads
@@ -1103,17 +1129,21 @@ __global__ void __launch_bounds__(kFetchThreads)
   __syncthreads();  // barrier initialised before anyone waits on it
   if (bulk && __syncthreads_or(!mbar_wait_bounded(&bar, 0, timeout_ns, fault))) return;
   for (int64_t c0 = lo; c0 < hi; c0 += kTile) {
-    int2 a[kFetchPer];
+    uint32_t ao[kFetchPer];
+    int32_t ai[kFetchPer];
 #pragma unroll
-    for (int e = 0; e < kFetchPer; ++e) a[e] = nxt[e];
+    for (int e = 0; e < kFetchPer; ++e) {
+      ao[e] = nxt_off[e];
+      ai[e] = nxt_i[e];
+    }
     if (c0 + kTile < hi) load(c0 + kTile);
     int2 pr[kFetchPer];
     int w[kFetchPer], rank[kFetchPer];
 #pragma unroll
     for (int e = 0; e < kFetchPer; ++e) {
       const bool valid = c0 + static_cast<int64_t>(e) * kFetchThreads + t < hi;
-      pr[e] = make_int2(a[e].y, valid ? win[a[e].x - base] : 0);  // {i, value}
-      w[e] = valid ? (a[e].y >> coarse_log) : -1;
+      pr[e] = make_int2(ai[e], valid ? win[ao[e]] : 0);  // {i, value}
+      w[e] = valid ? (ai[e] >> coarse_log) : -1;
       rank[e] = valid ? static_cast<int>(atomicAdd(&scnt[w[e]], 1u)) : -1;
     }
     __syncthreads();  // A
@@ -1166,8 +1196,11 @@ int ensure_win_attrs() {
   return st[dev];
 }
 
+// pairs_a: 8-byte pairs {x, y} (partition and fetch output); pairs_b: the
+// refine's output as 16-bit window offsets (at pairs_b) and 32-bit values
+// (at pairs_b + soa_val), both 16-byte aligned.
 struct TLayout {
-  size_t cnt, start, fill, cfill, fill2, cfill2, pairs_a, pairs_b, bytes;
+  size_t cnt, start, fill, cfill, fill2, cfill2, pairs_a, pairs_b, soa_val, bytes;
 };
 
 TLayout tlayout_of(int64_t n, const TPlan &p, bool gather) {
@@ -1185,7 +1218,8 @@ TLayout tlayout_of(int64_t n, const TPlan &p, bool gather) {
   L.fill2 = gather ? take(4 * static_cast<size_t>(p.F)) : 0;
   L.cfill2 = gather ? take(4 * static_cast<size_t>(p.C)) : 0;
   L.pairs_a = take(8 * static_cast<size_t>(n));
-  L.pairs_b = take(8 * static_cast<size_t>(n));
+  L.soa_val = round_up(2 * static_cast<size_t>(n), 256);
+  L.pairs_b = take(L.soa_val + 4 * static_cast<size_t>(n));
   L.bytes = o;
   return L;
 }
@@ -1213,7 +1247,8 @@ int tiled_run(const int32_t *in, int32_t *out, int64_t n, const int32_t *loc, in
   auto *fill2 = kScatter ? nullptr : reinterpret_cast<uint32_t *>(w + L.fill2);
   auto *cfill2 = kScatter ? nullptr : reinterpret_cast<uint32_t *>(w + L.cfill2);
   auto *pa = reinterpret_cast<int2 *>(w + L.pairs_a);
-  auto *pb = reinterpret_cast<int2 *>(w + L.pairs_b);
+  auto *pb_off = reinterpret_cast<uint16_t *>(w + L.pairs_b);
+  auto *pb_val = reinterpret_cast<int32_t *>(w + L.pairs_b + L.soa_val);
   if (cudaMemsetAsync(cnt, 0, 4 * static_cast<size_t>(p.F), st) != cudaSuccess) return EDPP_ECUDA;
   const int sms = device_sm_count();
   const bool vec_loc = aligned16(loc);
@@ -1231,19 +1266,21 @@ int tiled_run(const int32_t *in, int32_t *out, int64_t n, const int32_t *loc, in
   if (!fault) return EDPP_ECUDA;
   const int64_t rblocks = static_cast<int64_t>(sms) * kRefineBlocksPerSm;
   win_refine_kernel<<<static_cast<unsigned>(min64(tiles, rblocks)), kThreads, refine_smem(), st>>>(
-      pa, start + p.F, nullptr, 0, p.fine_log, p.coarse_log, tiles, fill, pb, kDefaultWaitNs, fault);
+      pa, start + p.F, nullptr, 0, p.fine_log, p.coarse_log, tiles, fill, pb_off, pb_val,
+      kDefaultWaitNs, fault);
   if (kScatter) {
     win_apply_kernel<<<static_cast<unsigned>(p.F), kWinThreads, apply_smem(p.fine_log), st>>>(
-        pb, start, nullptr, p.fine_log, n, out, aligned16(out), false);
+        pb_off, pb_val, start, nullptr, p.fine_log, n, out, aligned16(out), false);
   } else {
     win_fetch_kernel<<<static_cast<unsigned>(p.F), kFetchThreads, fetch_smem(p.fine_log, p.C), st>>>(
-        pb, start, in, n, p.fine_log, p.coarse_log, p.C, cfill2, pa, vec_in, kDefaultWaitNs, fault);
+        pb_off, pb_val, start, in, n, p.fine_log, p.coarse_log, p.C, cfill2, pa, vec_in,
+        kDefaultWaitNs, fault);
     const int64_t rtiles = static_cast<int64_t>(p.C) << (p.coarse_log - 12);
     win_refine_kernel<<<static_cast<unsigned>(min64(rtiles, rblocks)), kThreads, refine_smem(), st>>>(
-        pa, nullptr, cfill2, p.coarse_log, p.fine_log, p.coarse_log, rtiles, fill2, pb,
+        pa, nullptr, cfill2, p.coarse_log, p.fine_log, p.coarse_log, rtiles, fill2, pb_off, pb_val,
         kDefaultWaitNs, fault);
     win_apply_kernel<<<static_cast<unsigned>(p.F), kWinThreads, apply_smem(p.fine_log), st>>>(
-        pb, nullptr, fill2, p.fine_log, n, out, aligned16(out), true);
+        pb_off, pb_val, nullptr, fill2, p.fine_log, n, out, aligned16(out), true);
   }
   return launch_status();
 }

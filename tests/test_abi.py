@@ -58,9 +58,10 @@ def test_workspace_queries(edpp):
     assert lib.edpp_split_workspace_size(n, 4096, 2) >= 8 * n
     assert lib.edpp_split_workspace_size(n, 8192, 2) >= 8 * n
     assert lib.edpp_split_workspace_size(n, 1024, 2) < 8 * n
-    # the tiled gather/scatter: two pair arrays of 8 bytes per element
-    assert lib.edpp_gather_tiled_workspace_size(n) >= 16 * n
-    assert lib.edpp_scatter_tiled_workspace_size(n) >= 16 * n
+    # the tiled gather/scatter: one array of 8-byte pairs and one of 6-byte
+    # (16-bit window offset + 32-bit value) pairs per element
+    assert lib.edpp_gather_tiled_workspace_size(n) >= 14 * n
+    assert lib.edpp_scatter_tiled_workspace_size(n) >= 14 * n
 
 
 def test_argument_errors_before_any_device_work(edpp):
