@@ -117,8 +117,9 @@ template <int THREADS, int LAYOUT> size_t scatter_smem_bytes(int buckets) {
          static_cast<size_t>(ScatterCfg<THREADS>::kWarps) * std::min(buckets, 256);  // leaders
 }
 
+// Two blocks per SM (their staging fills shared memory): at most 64 registers.
 template <int THREADS, int LAYOUT>
-__global__ void __launch_bounds__(THREADS)
+__global__ void __launch_bounds__(THREADS, 2)
     split_scatter_kernel(const int32_t *__restrict__ keys_in, int32_t *__restrict__ keys_out,
                          const int32_t *__restrict__ vals_in, int32_t *__restrict__ vals_out,
                          int64_t n, int buckets, int shift, int64_t tiles,
@@ -260,20 +261,19 @@ __global__ void __launch_bounds__(THREADS)
   if (kbits <= 5 && lane < buckets) my_cnt[lane] = static_cast<uint16_t>(lane_cnt);
   __syncthreads();
 
-  // -- per bucket: exclusive prefix over warps, tile count, tile offsets --
+  // -- per bucket: tile count, tile offset, then each warp's first slot --
   // Thread-consecutive buckets so the block-wide scan over buckets is a
-  // per-thread serial scan plus one warp/ block combine.
+  // per-thread serial scan plus one warp/ block combine.  cnt16[w][b]
+  // becomes the tile slot of warp w's first element of bucket b (the
+  // bucket's tile offset plus the counts of the warps before w; < kTile, so
+  // it fits 16 bits), which leaves the re-layout one lookup per element.
   int32_t my_total = 0;
   for (int b = b_lo; b < b_hi; ++b) {
-    int32_t run = 0;
+    int32_t tot = 0;
 #pragma unroll 4
-    for (int ww = 0; ww < C::kWarps; ++ww) {
-      const int32_t c = cnt16[ww * buckets + b];
-      cnt16[ww * buckets + b] = static_cast<uint16_t>(run);
-      run += c;
-    }
-    toff[b] = run;  // tile count for now
-    my_total += run;
+    for (int ww = 0; ww < C::kWarps; ++ww) tot += cnt16[ww * buckets + b];
+    toff[b] = tot;  // tile count for now
+    my_total += tot;
   }
   // Block exclusive scan of my_total.
   __shared__ int32_t s_wsum[32];
@@ -297,21 +297,29 @@ __global__ void __launch_bounds__(THREADS)
   }
   __syncthreads();
   int32_t run = s_wsum[w] + (incl - my_total);
+  auto warp_slots = [&](int b, int32_t start) {
+#pragma unroll 4
+    for (int ww = 0; ww < C::kWarps; ++ww) {
+      const int32_t c = cnt16[ww * buckets + b];
+      cnt16[ww * buckets + b] = static_cast<uint16_t>(start);
+      start += c;
+    }
+  };
 #pragma unroll
   for (int k = 0; k < kHisPre; ++k) {
     const int b = b_lo + k;
     if (b < b_hi) {
       const int32_t c = toff[b];
-      toff[b] = run;
       // First output index of bucket b from this tile, minus its tile offset.
       gofs[b] = his_pre[k] - run;
+      warp_slots(b, run);
       run += c;
     }
   }
   for (int b = b_lo + kHisPre; b < b_hi; ++b) {
     const int32_t c = toff[b];
-    toff[b] = run;
     gofs[b] = his[static_cast<int64_t>(b) * tiles + t] - run;
+    warp_slots(b, run);
     run += c;
   }
   __syncthreads();
@@ -328,8 +336,7 @@ __global__ void __launch_bounds__(THREADS)
       if (pos < count) {
         const int b = static_cast<int>((static_cast<unsigned>(kk[it]) >> shift) & mask);
         const int r = static_cast<int>((rk[it >> 1] >> ((it & 1) * 16)) & 0xffffu);
-        const int64_t o =
-            static_cast<int64_t>(gofs[b]) + toff[b] + cnt16[w * buckets + b] + r;
+        const int64_t o = static_cast<int64_t>(gofs[b]) + cnt16[w * buckets + b] + r;
         if (LAYOUT == EDPP_KVS_AOS) {
           reinterpret_cast<int2 *>(keys_out)[o] = make_int2(kk[it], vv[it]);
         } else {
@@ -348,7 +355,7 @@ __global__ void __launch_bounds__(THREADS)
     if (pos < count) {
       const int b = static_cast<int>((static_cast<unsigned>(kk[it]) >> shift) & mask);
       const int r = static_cast<int>((rk[it >> 1] >> ((it & 1) * 16)) & 0xffffu);
-      const int s = toff[b] + cnt16[w * buckets + b] + r;
+      const int s = cnt16[w * buckets + b] + r;
       if (LAYOUT == EDPP_KVS_AOS) {
         s_pairs[s] = make_int2(kk[it], vv[it]);
       } else {
