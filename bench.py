@@ -772,6 +772,59 @@ def run_split_workload(args, rank, world):
     return 0
 
 
+def run_autotune_workload(args, rank, world):
+    """Per-size-class autotuning of the plain primitives: for every size
+    class, time each look-back tile shape and each slice length of the
+    chunked reduce-then-scan (int32 and int64), and the gather's tiled form
+    against its direct sweep, on seeded data; record the winners and write
+    the table (--tune-out, default the committed
+    efficient-dpp_gb300/tuning/plain_gb300.tsv).  Prints every variant's time."""
+    import torch
+
+    import edpp
+    edpp.lib()
+    dev = _device(args)
+    if rank != 0:
+        return 0
+    edpp.lib().edpp_tune_clear()
+    reps = max(3, args.steps)
+    rows = []
+    plan = [(edpp.TUNE_SCAN_LOOKBACK, "int32", range(16, 31, 2)),
+            (edpp.TUNE_SCAN_LOOKBACK, "int64", range(16, 30, 2)),
+            (edpp.TUNE_SCAN_RTS, "int32", range(25, 31)),
+            (edpp.TUNE_SCAN_RTS, "int64", range(24, 30)),
+            (edpp.TUNE_GATHER, "int32", (20, 22, 24, 25, 26, 27, 28))]
+    for prim, dt, logs in plan:
+        for lg in logs:
+            n = 1 << lg
+            tdt = getattr(torch, dt)
+            if prim == edpp.TUNE_GATHER:
+                x = torch.arange(n, dtype=tdt, device=dev)
+                loc = torch.from_numpy(edpp.gen_permutation(n, 2)).to(dev)
+                ws = edpp.workspace(edpp.gs_workspace_bytes("gather", n, 1, "tiled"), dev)
+            else:
+                x = torch.randint(0, 101, (n,), dtype=tdt, device=dev)
+                loc = None
+                algo = "lookback" if prim == edpp.TUNE_SCAN_LOOKBACK else "rts"
+                ws = edpp.workspace(edpp.scan_workspace_bytes(n, dt, algo), dev)
+            y = torch.empty_like(x)
+            v, ms, each = edpp.autotune_plain(prim, x, y, ws, loc=loc, reps=reps)
+            rows.append({"primitive": edpp.TUNE_NAMES[prim], "dtype": dt, "log2n": lg,
+                         "best": v, "ms": [round(m, 4) for m in each]})
+            del x, y, ws, loc
+            torch.cuda.empty_cache()
+    if edpp.sync_status() != edpp.EDPP_OK:
+        raise SystemExit("device fault in the autotune workload")
+    out = args.tune_out or str(PKG / "tuning" / "plain_gb300.tsv")
+    edpp.tune_save(out)
+    print(json.dumps({"metric": METRIC, "workload_metric": "autotune table (ms per variant)",
+                      "value": None, "unit": "ms", "n_gpus": world, "steps": reps,
+                      "warmup": 1, "higher_is_better": False, "data": "synthetic",
+                      "config": {"workload": "per-size-class autotune of the plain primitives"},
+                      "table": out, "rows": rows}), flush=True)
+    return 0
+
+
 def run_radix_workload(args, rank, world):
     """LSD radix sort on the stable split (8-bit digits): 2^k uniform int32 keys
     (seed 3), keys only and with int32 values, against torch.sort(stable=True)
@@ -969,7 +1022,7 @@ def main(argv=None):
                     help="skip timing the other gather/scatter schedule")
     ap.add_argument("--workload", default="gs_stream",
                     choices=["gs_stream", "batch", "serve", "scan", "split", "join", "access",
-                             "radix"],
+                             "radix", "autotune"],
                     help="gs_stream: multi-pass gather/scatter + STREAM (default); "
                          "batch: 4096 uneven segments, batched vs plain; "
                          "serve: Poisson request stream through the server")
@@ -990,6 +1043,8 @@ def main(argv=None):
                     help="scan: only the config-1 rows")
     ap.add_argument("--autotune", action="store_true",
                     help="batch: run the autotuner and record its choice")
+    ap.add_argument("--tune-out", default="",
+                    help="autotune: where to write the plain primitives' table")
     args = ap.parse_args(argv)
     args.warmup = max(args.warmup, 3)
 
@@ -1010,6 +1065,8 @@ def main(argv=None):
         return run_radix_workload(args, rank, world)
     if args.workload == "access":
         return run_access_workload(args, rank, world)
+    if args.workload == "autotune":
+        return run_autotune_workload(args, rank, world)
 
     import numpy as np
     import torch

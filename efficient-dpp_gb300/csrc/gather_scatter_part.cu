@@ -28,6 +28,7 @@
 #include <mutex>
 
 #include "common.cuh"
+#include "tune.h"
 
 namespace edpp {
 namespace {
@@ -1333,11 +1334,13 @@ int edpp_scatter_i32_tiled(const int32_t *in, int32_t *out, int64_t length, cons
 }
 
 int edpp_gather_prefers_direct(int64_t length) {
-  // A gather whose source is at most ~2.5x L2 keeps enough of it in L2 that
-  // the direct random sweep wins (measured, int32 permutations: 2^25 0.49 ms
-  // direct against 0.59 ms tiled; 2^26 1.00 against 1.10; 2^28 5.34
-  // against 4.32).
-  return static_cast<double>(length) * 4.0 <= 2.5 * static_cast<double>(edpp::device_l2_bytes());
+  // Without a tuning entry: a gather whose source is at most ~2.5x L2 keeps
+  // enough of it in L2 that the direct random sweep wins (measured, int32
+  // permutations: 2^25 0.49 ms direct against 0.59 ms tiled; 2^26 1.00
+  // against 1.10; 2^28 5.34 against 4.32).
+  const bool rule =
+      static_cast<double>(length) * 4.0 <= 2.5 * static_cast<double>(edpp::device_l2_bytes());
+  return edpp::tuned_variant(EDPP_TUNE_GATHER, 4, length, rule ? 1 : 0) == 1;
 }
 
 }  // extern "C"

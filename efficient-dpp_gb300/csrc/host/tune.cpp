@@ -1,0 +1,248 @@
+// tune.cpp — per-size-class tuning table of the plain primitives and the
+// autotuner that fills it.
+//
+// Entries map (primitive, element size, log2 of the length) to a variant.
+// The primitives look their size up at call time (tuned_variant); a length
+// between recorded classes takes the nearest one.  The committed table,
+// efficient-dpp_gb300/tuning/plain_gb300.tsv, is read on first use from
+// beside the library's lib/ directory (found with dladdr).  The reference
+// picks its tunables by hand per device (opencl/test/test_scan_global.cpp:
+// 87-94: R, L, local and grid of scan_chained); here they are timed on the
+// device by edpp_autotune_plain and recorded.
+#include <dlfcn.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "edpp.h"
+#include "tune.h"
+
+namespace edpp {
+namespace {
+
+struct Entry {
+  int prim, elem, cls, variant;
+  float ms;
+};
+
+const char *const kNames[] = {"scan_lookback", "scan_rts", "gather"};
+constexpr int kPrims = 3;
+
+std::mutex g_mu;
+std::vector<Entry> g_table;
+bool g_loaded = false;
+
+int prim_of(const char *name) {
+  for (int p = 0; p < kPrims; ++p)
+    if (std::strcmp(name, kNames[p]) == 0) return p;
+  return -1;
+}
+
+int variants_of(int prim) {
+  switch (prim) {
+    case EDPP_TUNE_SCAN_LOOKBACK: return scan_variants(EDPP_SCAN_LOOKBACK);
+    case EDPP_TUNE_SCAN_RTS: return scan_variants(EDPP_SCAN_RTS);
+    case EDPP_TUNE_GATHER: return 2;
+    default: return 0;
+  }
+}
+
+int class_of(int64_t n) {
+  int c = 0;
+  while (c < 62 && (int64_t{1} << (c + 1)) <= n) ++c;
+  return c;
+}
+
+// efficient-dpp_gb300/tuning/plain_gb300.tsv, from this library's path
+// efficient-dpp_gb300/lib/libedpp.so.
+std::string default_path() {
+  Dl_info info;
+  if (dladdr(reinterpret_cast<void *>(&edpp_tune_variants), &info) == 0 || !info.dli_fname)
+    return {};
+  std::string p(info.dli_fname);
+  const size_t a = p.rfind('/');
+  if (a == std::string::npos) return "../tuning/plain_gb300.tsv";
+  const std::string lib_dir = p.substr(0, a);
+  const size_t b = lib_dir.rfind('/');
+  const std::string pkg = b == std::string::npos ? std::string(".") : lib_dir.substr(0, b);
+  return pkg + "/tuning/plain_gb300.tsv";
+}
+
+void set_locked(int prim, int elem, int cls, int variant, float ms) {
+  for (Entry &e : g_table)
+    if (e.prim == prim && e.elem == elem && e.cls == cls) {
+      e.variant = variant;
+      e.ms = ms;
+      return;
+    }
+  g_table.push_back({prim, elem, cls, variant, ms});
+}
+
+int load_locked(const std::string &path) {
+  g_table.clear();
+  g_loaded = true;
+  if (path.empty()) return EDPP_OK;
+  FILE *f = std::fopen(path.c_str(), "r");
+  if (!f) return EDPP_OK;  // no table: every primitive takes its default
+  char line[256];
+  int status = EDPP_OK;
+  while (std::fgets(line, sizeof line, f)) {
+    char *hash = std::strchr(line, '#');
+    if (hash) *hash = '\0';
+    char name[64];
+    int elem = 0, cls = 0, variant = 0;
+    float ms = 0.0f;
+    const int got = std::sscanf(line, "%63s %d %d %d %f", name, &elem, &cls, &variant, &ms);
+    if (got <= 0) continue;  // blank or comment
+    const int prim = got >= 4 ? prim_of(name) : -1;
+    if (prim < 0 || (elem != 4 && elem != 8) || cls < 0 || cls > 62 || variant < 0 ||
+        variant >= variants_of(prim)) {
+      status = EDPP_EINVAL;  // a malformed line is skipped and reported
+      continue;
+    }
+    set_locked(prim, elem, cls, variant, got >= 5 ? ms : 0.0f);
+  }
+  std::fclose(f);
+  return status;
+}
+
+void ensure_loaded_locked() {
+  if (!g_loaded) load_locked(default_path());
+}
+
+}  // namespace
+
+int tuned_variant(int prim, int elem_bytes, int64_t length, int fallback) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  ensure_loaded_locked();
+  const int cls = class_of(length);
+  const Entry *best = nullptr;
+  for (const Entry &e : g_table) {
+    if (e.prim != prim || e.elem != elem_bytes) continue;
+    if (!best || std::abs(e.cls - cls) < std::abs(best->cls - cls) ||
+        (std::abs(e.cls - cls) == std::abs(best->cls - cls) && e.cls > best->cls))
+      best = &e;
+  }
+  return best ? best->variant : fallback;
+}
+
+}  // namespace edpp
+
+extern "C" {
+
+int edpp_tune_variants(int primitive) { return edpp::variants_of(primitive); }
+
+int edpp_tune_set(int primitive, int elem_bytes, int log2_length, int variant, float ms) {
+  if (primitive < 0 || primitive >= edpp::kPrims || (elem_bytes != 4 && elem_bytes != 8) ||
+      log2_length < 0 || log2_length > 62 || variant < 0 ||
+      variant >= edpp::variants_of(primitive))
+    return EDPP_EINVAL;
+  std::lock_guard<std::mutex> lk(edpp::g_mu);
+  edpp::ensure_loaded_locked();
+  edpp::set_locked(primitive, elem_bytes, log2_length, variant, ms);
+  return EDPP_OK;
+}
+
+int edpp_tune_get(int primitive, int elem_bytes, int64_t length, int *variant) {
+  if (!variant || primitive < 0 || primitive >= edpp::kPrims) return EDPP_EINVAL;
+  const int v = edpp::tuned_variant(primitive, elem_bytes, length, -1);
+  *variant = v < 0 ? 0 : v;
+  return v < 0 ? EDPP_EINVAL : EDPP_OK;
+}
+
+int edpp_tune_load(const char *path) {
+  std::lock_guard<std::mutex> lk(edpp::g_mu);
+  return edpp::load_locked(path ? std::string(path) : edpp::default_path());
+}
+
+int edpp_tune_save(const char *path) {
+  if (!path) return EDPP_EINVAL;
+  std::lock_guard<std::mutex> lk(edpp::g_mu);
+  edpp::ensure_loaded_locked();
+  FILE *f = std::fopen(path, "w");
+  if (!f) return EDPP_EINVAL;
+  std::fprintf(f,
+               "# Per-size-class choices of the plain primitives (edpp_autotune_plain).\n"
+               "# primitive  elem_bytes  log2_length  variant  ms\n");
+  std::vector<edpp::Entry> rows = edpp::g_table;
+  for (size_t i = 1; i < rows.size(); ++i)  // stable order: primitive, element size, class
+    for (size_t j = i; j > 0; --j) {
+      const edpp::Entry &a = rows[j - 1], &b = rows[j];
+      if (std::make_tuple(a.prim, a.elem, a.cls) <= std::make_tuple(b.prim, b.elem, b.cls)) break;
+      std::swap(rows[j - 1], rows[j]);
+    }
+  for (const edpp::Entry &e : rows)
+    std::fprintf(f, "%s %d %d %d %.4f\n", edpp::kNames[e.prim], e.elem, e.cls, e.variant, e.ms);
+  return std::fclose(f) == 0 ? EDPP_OK : EDPP_EINVAL;
+}
+
+void edpp_tune_clear(void) {
+  std::lock_guard<std::mutex> lk(edpp::g_mu);
+  edpp::g_table.clear();
+  edpp::g_loaded = true;
+}
+
+int edpp_autotune_plain(int primitive, const void *in, void *out, const int32_t *loc,
+                        int64_t length, int elem_bytes, void *ws, size_t ws_bytes, void *stream,
+                        int reps, int *best_variant, float *best_ms, float *variant_ms) {
+  const int nv = edpp::variants_of(primitive);
+  if (nv <= 0 || !best_variant || reps < 1 || length <= 0 || !in || !out) return EDPP_EINVAL;
+  if (primitive == EDPP_TUNE_GATHER && (!loc || elem_bytes != 4)) return EDPP_EINVAL;
+  if (elem_bytes != 4 && elem_bytes != 8) return EDPP_EINVAL;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  auto run = [&](int v) {
+    switch (primitive) {
+      case EDPP_TUNE_SCAN_LOOKBACK:
+        return edpp::scan_with_variant(in, out, length, elem_bytes, EDPP_SCAN_LOOKBACK, v, ws,
+                                       ws_bytes, stream);
+      case EDPP_TUNE_SCAN_RTS:
+        return edpp::scan_with_variant(in, out, length, elem_bytes, EDPP_SCAN_RTS, v, ws, ws_bytes,
+                                       stream);
+      default: {
+        const int32_t *src = static_cast<const int32_t *>(in);
+        int32_t *dst = static_cast<int32_t *>(out);
+        return v == 1 ? edpp_gather_i32(src, dst, length, loc, 1, stream)
+                      : edpp_gather_i32_tiled(src, dst, length, loc, 1, ws, ws_bytes, stream);
+      }
+    }
+  };
+  cudaEvent_t a, b;
+  if (cudaEventCreate(&a) != cudaSuccess) return EDPP_ECUDA;
+  if (cudaEventCreate(&b) != cudaSuccess) {
+    cudaEventDestroy(a);
+    return EDPP_ECUDA;
+  }
+  int status = EDPP_OK, best = -1;
+  float best_t = 0.0f;
+  for (int v = 0; v < nv && status == EDPP_OK; ++v) {
+    status = run(v);  // warm-up
+    if (status == EDPP_OK && cudaEventRecord(a, st) != cudaSuccess) status = EDPP_ECUDA;
+    for (int r = 0; r < reps && status == EDPP_OK; ++r) status = run(v);
+    if (status == EDPP_OK && cudaEventRecord(b, st) != cudaSuccess) status = EDPP_ECUDA;
+    if (status == EDPP_OK) status = edpp_sync_status(stream, 0);
+    float ms = 0.0f;
+    if (status == EDPP_OK && cudaEventElapsedTime(&ms, a, b) != cudaSuccess) status = EDPP_ECUDA;
+    if (status != EDPP_OK) break;
+    ms /= static_cast<float>(reps);
+    if (variant_ms) variant_ms[v] = ms;
+    if (best < 0 || ms < best_t) {
+      best = v;
+      best_t = ms;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (status != EDPP_OK) return status;
+  *best_variant = best;
+  if (best_ms) *best_ms = best_t;
+  return edpp_tune_set(primitive, elem_bytes, edpp::class_of(length), best, best_t);
+}
+
+}  // extern "C"

@@ -28,6 +28,7 @@
 #include <mutex>
 
 #include "scan_tile.cuh"
+#include "tune.h"
 
 namespace edpp {
 namespace {
@@ -42,10 +43,19 @@ constexpr size_t kHeader = 256;
 constexpr int64_t kMaxChunkBlocks = 8192;
 
 template <typename T> using TS = TileScan<T, kThreads, kChunks>;
-// The look-back kernel runs the same 16 KB tiles with 4 warps of 8 chunks:
-// fewer warps idle at the barrier while warp 0 looks back.
+// Look-back tile shapes (threads per block, 16-byte chunks per thread, blocks
+// per SM for 4- / 8-byte elements), chosen per size class by the tuning
+// table (edpp_tune_*):
+//   variant 0  128 x 8   16 KB tiles, 12 / 8 blocks per SM (the default:
+//              fewer warps idle at the barrier while warp 0 looks back)
+//   variant 1  256 x 8   32 KB tiles,  6 / 4 blocks per SM (half the tiles,
+//              so half the look-backs)
+//   variant 2  512 x 4   32 KB tiles,  6 / 4 blocks per SM
+// Variant 0's tiles are the smallest; tile state and workspace are sized
+// for them, so every shape fits the same workspace.
 constexpr int kLbThreads = 128;
 constexpr int kLbChunks = 8;
+constexpr int kLbVariants = 3;
 template <typename T> using TSL = TileScan<T, kLbThreads, kLbChunks>;
 static_assert(TSL<int32_t>::kTile == TS<int32_t>::kTile && TSL<int64_t>::kTile == TS<int64_t>::kTile,
               "look-back tiles match the other schemes' tiles");
@@ -57,12 +67,13 @@ static_assert(TSL<int32_t>::kTile == TS<int32_t>::kTile && TSL<int64_t>::kTile =
 // Measured at 2^30 int32 against an atomic tile ticket and 8 blocks of 256
 // threads: block-index tiles 13% faster, then 12 blocks of 128 threads per
 // SM another 12%.
-template <typename T, bool kInclusive>
-__global__ void __launch_bounds__(kLbThreads, sizeof(T) == 4 ? 12 : 8)
+template <typename T, bool kInclusive, int TH = kLbThreads, int CH = kLbChunks,
+          int MINB = (sizeof(T) == 4 ? 12 : 8)>
+__global__ void __launch_bounds__(TH, MINB)
     scan_lookback_kernel(const T *in, T *out, int64_t n, int64_t num_tiles,
                          unsigned long long *ticket, LookbackState<T> st, int64_t tile_base,
                          bool tma, bool vec_out, uint64_t timeout_ns, unsigned *fault) {
-  using S = TSL<T>;
+  using S = TileScan<T, TH, CH>;
   constexpr int kTile = S::kTile;
   __shared__ alignas(128) T tile[kTile];
   __shared__ typename S::Shared sh;
@@ -81,14 +92,14 @@ __global__ void __launch_bounds__(kLbThreads, sizeof(T) == 4 ? 12 : 8)
   const int64_t base = t * kTile;
   const int count = static_cast<int>(min64(kTile, n - base));
 
-  const uint32_t bulk = stage_tile<T, kTile, kLbThreads>(tile, in + base, count, tma, &bar);
+  const uint32_t bulk = stage_tile<T, kTile, TH>(tile, in + base, count, tma, &bar);
   if (bulk) {
     if (!mbar_wait_bounded(&bar, 0, timeout_ns, fault)) return;
   }
   if (count < kTile || !bulk) __syncthreads();
 
-  Chunk<T> c[kLbChunks];
-  T wex[kLbChunks];
+  Chunk<T> c[CH];
+  T wex[CH];
   S::phase1(tile, c, wex, sh);
   __syncthreads();
   if (threadIdx.x < 32) {
@@ -361,9 +372,14 @@ __global__ void __launch_bounds__(kThreads)
 // one count per chunk, a whole iteration after it started filling.  Waits are
 // bounded; a block that gives up raises EDPP_FAULT_TIMEOUT and sets the
 // call's abort flag so the others stop too.
-constexpr int kSliceTiles = 2;
+// kSliceTiles is the slice length in tiles, chosen per size class by the
+// tuning table: variant 0 two tiles (the default), variant 1 one tile,
+// variant 2 four tiles (reduced in two rounds of eight 16-byte loads per
+// thread).  The workspace is sized for one-tile slices, the most.
+constexpr int kRtsVariants = 3;
+constexpr int rts_slice_tiles(int variant) { return variant == 1 ? 1 : variant == 2 ? 4 : 2; }
 
-template <typename T, bool kInclusive>
+template <typename T, bool kInclusive, int kSliceTiles>
 __global__ void __launch_bounds__(kThreads, 4)
     rts_chunked_kernel(const T *in, T *out, int64_t n, int64_t chunks, T *sums, unsigned *cnt,
                        unsigned *abort_flag, bool tma, bool vec_out, uint64_t timeout_ns,
@@ -388,18 +404,22 @@ __global__ void __launch_bounds__(kThreads, 4)
     const int64_t hi = min64(n, lo + kSliceTiles * kTile);
     T v;
     if (tma && hi - lo == kSliceTiles * kTile) {
-      // a whole slice: every 16-byte load of the slice in flight at once
+      // a whole slice: up to eight 16-byte loads per thread in flight at once
       constexpr int kV = kSliceTiles * kChunks;
+      constexpr int kRound = kV < 8 ? kV : 8;
       constexpr int E = Chunk<T>::E;
       const uint4 *p = reinterpret_cast<const uint4 *>(in + lo);
-      Chunk<T> q[kV];
-#pragma unroll
-      for (int k = 0; k < kV; ++k) q[k].raw = __ldcg(p + k * kThreads + tid);
       T acc = zero_of<T>();
 #pragma unroll
-      for (int k = 0; k < kV; ++k)
+      for (int r0 = 0; r0 < kV; r0 += kRound) {
+        Chunk<T> q[kRound];
 #pragma unroll
-        for (int e = 0; e < E; ++e) acc = op_add(acc, q[k].e[e]);
+        for (int k = 0; k < kRound; ++k) q[k].raw = __ldcg(p + (r0 + k) * kThreads + tid);
+#pragma unroll
+        for (int k = 0; k < kRound; ++k)
+#pragma unroll
+          for (int e = 0; e < E; ++e) acc = op_add(acc, q[k].e[e]);
+      }
       acc = warp_sum(acc);
       if ((tid & 31) == 0) s_red[0][tid >> 5] = acc;
       __syncthreads();
@@ -518,9 +538,10 @@ template <typename T> int64_t tiles_of(int64_t n) {
 }
 
 // The chunked RTS: chunks * G slice sums (chunks * G <= slices + G) and one
-// count per chunk (chunks <= slices), after the header.
-template <typename T> int64_t slices_of(int64_t n) {
-  return (tiles_of<T>(n) + kSliceTiles - 1) / kSliceTiles;
+// count per chunk (chunks <= slices), after the header; sized for the
+// shortest slices (one tile).
+template <typename T> int64_t slices_of(int64_t n, int slice_tiles = 1) {
+  return (tiles_of<T>(n) + slice_tiles - 1) / slice_tiles;
 }
 template <typename T> size_t chunked_sums_bytes(int64_t n) {
   return round_up(static_cast<size_t>(slices_of<T>(n) + kMaxChunkBlocks) * sizeof(T), 256);
@@ -547,9 +568,71 @@ template <typename T> void chunk_grid(int64_t n, int64_t &blocks, int64_t &tpb) 
   blocks = (tiles + tpb - 1) / tpb;
 }
 
+// One look-back launch with tile shape TH x CH (MINB4 / MINB8 blocks per SM
+// for 4- / 8-byte elements).  Zeroes the header and the state it uses.
+template <typename T, bool kInclusive, int TH, int CH, int MINB4, int MINB8>
+int launch_lookback(const T *in, T *out, int64_t n, char *w, cudaStream_t st, int64_t tile_base,
+                    bool tma, bool vec_out, uint64_t timeout_ns, unsigned *fault) {
+  constexpr int64_t kTileS = TileScan<T, TH, CH>::kTile;
+  const int64_t tiles = (n + kTileS - 1) / kTileS;
+  if (cudaMemsetAsync(w, 0, kHeader + LookbackState<T>::bytes(tiles), st) != cudaSuccess)
+    return EDPP_ECUDA;
+  LookbackState<T> state;
+  state.bind(w + kHeader, tiles);
+  // One block per tile, in block-index order.  (A persistent form that
+  // prefetches its next tile measured 10-15% slower: look-backs of blocks
+  // that advance in lockstep see fewer published prefixes.)
+  scan_lookback_kernel<T, kInclusive, TH, CH, sizeof(T) == 4 ? MINB4 : MINB8>
+      <<<static_cast<unsigned>(tiles), TH, 0, st>>>(in, out, n, tiles,
+                                                     reinterpret_cast<unsigned long long *>(w),
+                                                     state, tile_base, tma, vec_out, timeout_ns,
+                                                     fault);
+  return launch_status();
+}
+
+// The chunked reduce-then-scan with slices of kSlice tiles, as one
+// cooperative launch; EDPP_ENOMEM (a fallback signal, nothing launched) when
+// the kernel cannot be resident on this device.
+template <typename T, bool kInclusive, int kSlice>
+int launch_rts_chunked(const T *in, T *out, int64_t n, char *w, cudaStream_t st, bool tma,
+                       bool vec_out, uint64_t timeout_ns, unsigned *fault) {
+  static int cresident[64];
+  static std::once_flag conce[64];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  std::call_once(conce[dev], [dev] {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &per_sm, rts_chunked_kernel<T, kInclusive, kSlice>, kThreads, 0) != cudaSuccess)
+      per_sm = 0;
+    cresident[dev] = per_sm * device_sm_count();
+  });
+  if (cresident[dev] <= 0) return EDPP_ENOMEM;
+  const int64_t slices = slices_of<T>(n, kSlice);
+  const int64_t g = std::min<int64_t>({slices, cresident[dev], kMaxChunkBlocks});
+  const int64_t chunks = (slices + g - 1) / g;
+  T *sums = reinterpret_cast<T *>(w + kHeader);
+  unsigned *cnt = reinterpret_cast<unsigned *>(w + kHeader + chunked_sums_bytes<T>(n));
+  if (cudaMemsetAsync(w, 0, kHeader, st) != cudaSuccess ||
+      cudaMemsetAsync(cnt, 0, sizeof(unsigned) * static_cast<size_t>(chunks), st) != cudaSuccess)
+    return EDPP_ECUDA;
+  unsigned *abort_flag = reinterpret_cast<unsigned *>(w + 8);
+  int64_t n_arg = n, chunks_arg = chunks;
+  bool tma_arg = tma, vec_arg = vec_out;
+  uint64_t to_arg = timeout_ns;
+  void *args[] = {const_cast<T **>(&in), &out, &n_arg, &chunks_arg, &sums, &cnt, &abort_flag,
+                  &tma_arg, &vec_arg, &to_arg, &fault};
+  cudaLaunchCooperativeKernel(
+      reinterpret_cast<const void *>(rts_chunked_kernel<T, kInclusive, kSlice>),
+      dim3(static_cast<unsigned>(g)), dim3(kThreads), args, 0, st);
+  return launch_status();
+}
+
+// variant < 0: the tuning table's choice for this size (else the default).
 template <typename T, bool kInclusive>
 int scan_impl(const T *in, T *out, int64_t n, int algo, void *ws, size_t ws_bytes, void *stream,
-              int64_t tile_base = 0, uint64_t timeout_ns = kDefaultWaitNs) {
+              int64_t tile_base = 0, uint64_t timeout_ns = kDefaultWaitNs, int variant = -1) {
   if (n < 0) return EDPP_EINVAL;
   if (algo != EDPP_SCAN_LOOKBACK && algo != EDPP_SCAN_RTS && algo != EDPP_SCAN_SSA)
     return EDPP_EINVAL;
@@ -565,17 +648,18 @@ int scan_impl(const T *in, T *out, int64_t n, int algo, void *ws, size_t ws_byte
   char *w = static_cast<char *>(ws);
 
   if (algo == EDPP_SCAN_LOOKBACK) {
-    const int64_t tiles = tiles_of<T>(n);
-    if (cudaMemsetAsync(ws, 0, need, st) != cudaSuccess) return EDPP_ECUDA;
-    LookbackState<T> state;
-    state.bind(w + kHeader, tiles);
-    // One block per tile, in block-index order.  (A persistent form
-    // that prefetches its next tile measured 10-15% slower: look-backs of
-    // blocks that advance in lockstep see fewer published prefixes.)
-    scan_lookback_kernel<T, kInclusive><<<static_cast<unsigned>(tiles), kLbThreads, 0, st>>>(
-        in, out, n, tiles, reinterpret_cast<unsigned long long *>(w), state, tile_base, tma,
-        vec_out, timeout_ns, fault);
-    return launch_status();
+    if (variant < 0) variant = tuned_variant(EDPP_TUNE_SCAN_LOOKBACK, sizeof(T), n, 0);
+    switch (variant) {
+      case 1:
+        return launch_lookback<T, kInclusive, 256, 8, 6, 4>(in, out, n, w, st, tile_base, tma,
+                                                            vec_out, timeout_ns, fault);
+      case 2:
+        return launch_lookback<T, kInclusive, 512, 4, 6, 4>(in, out, n, w, st, tile_base, tma,
+                                                            vec_out, timeout_ns, fault);
+      default:
+        return launch_lookback<T, kInclusive, kLbThreads, kLbChunks, 12, 8>(
+            in, out, n, w, st, tile_base, tma, vec_out, timeout_ns, fault);
+    }
   }
 
   int64_t blocks, tpb;
@@ -619,39 +703,22 @@ int scan_impl(const T *in, T *out, int64_t n, int algo, void *ws, size_t ws_byte
   if (algo == EDPP_SCAN_RTS) {
     // larger than L2: the chunked one-launch form, which reads each element
     // from DRAM once
-    static int cresident[64];
-    static std::once_flag conce[64];
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (dev < 0 || dev >= 64) dev = 0;
-    std::call_once(conce[dev], [dev] {
-      int per_sm = 0;
-      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-              &per_sm, rts_chunked_kernel<T, kInclusive>, kThreads, 0) != cudaSuccess)
-        per_sm = 0;
-      cresident[dev] = per_sm * device_sm_count();
-    });
-    if (cresident[dev] > 0) {
-      const int64_t slices = slices_of<T>(n);
-      const int64_t g = std::min<int64_t>({slices, cresident[dev], kMaxChunkBlocks});
-      const int64_t chunks = (slices + g - 1) / g;
-      T *sums = reinterpret_cast<T *>(w + kHeader);
-      unsigned *cnt = reinterpret_cast<unsigned *>(w + kHeader + chunked_sums_bytes<T>(n));
-      if (cudaMemsetAsync(w, 0, kHeader, st) != cudaSuccess ||
-          cudaMemsetAsync(cnt, 0, sizeof(unsigned) * static_cast<size_t>(chunks), st) !=
-              cudaSuccess)
-        return EDPP_ECUDA;
-      unsigned *abort_flag = reinterpret_cast<unsigned *>(w + 8);
-      int64_t n_arg = n, chunks_arg = chunks;
-      bool tma_arg = tma, vec_arg = vec_out;
-      uint64_t to_arg = timeout_ns;
-      void *args[] = {const_cast<T **>(&in), &out, &n_arg, &chunks_arg, &sums, &cnt, &abort_flag,
-                      &tma_arg, &vec_arg, &to_arg, &fault};
-      cudaLaunchCooperativeKernel(
-          reinterpret_cast<const void *>(rts_chunked_kernel<T, kInclusive>),
-          dim3(static_cast<unsigned>(g)), dim3(kThreads), args, 0, st);
-      return launch_status();
+    if (variant < 0) variant = tuned_variant(EDPP_TUNE_SCAN_RTS, sizeof(T), n, 0);
+    int s;
+    switch (variant) {
+      case 1:
+        s = launch_rts_chunked<T, kInclusive, 1>(in, out, n, w, st, tma, vec_out, timeout_ns,
+                                                 fault);
+        break;
+      case 2:
+        s = launch_rts_chunked<T, kInclusive, 4>(in, out, n, w, st, tma, vec_out, timeout_ns,
+                                                 fault);
+        break;
+      default:
+        s = launch_rts_chunked<T, kInclusive, 2>(in, out, n, w, st, tma, vec_out, timeout_ns,
+                                                 fault);
     }
+    if (s != EDPP_ENOMEM) return s;
     reduce_blocks_kernel<T><<<static_cast<unsigned>(blocks), kThreads, 0, st>>>(in, n, per,
                                                                                 partials, tma);
     scan_partials_kernel<T><<<1, 1024, 0, st>>>(partials, static_cast<int>(blocks));
@@ -668,6 +735,25 @@ int scan_impl(const T *in, T *out, int64_t n, int algo, void *ws, size_t ws_byte
 }
 
 }  // namespace
+
+int scan_with_variant(const void *in, void *out, int64_t length, int elem_bytes, int algo,
+                      int variant, void *ws, size_t ws_bytes, void *stream) {
+  if (variant < 0 || variant >= scan_variants(algo)) return EDPP_EINVAL;
+  if (elem_bytes == 4)
+    return scan_impl<int32_t, false>(static_cast<const int32_t *>(in), static_cast<int32_t *>(out),
+                                     length, algo, ws, ws_bytes, stream, 0, kDefaultWaitNs,
+                                     variant);
+  if (elem_bytes == 8)
+    return scan_impl<int64_t, false>(static_cast<const int64_t *>(in), static_cast<int64_t *>(out),
+                                     length, algo, ws, ws_bytes, stream, 0, kDefaultWaitNs,
+                                     variant);
+  return EDPP_EINVAL;
+}
+
+int scan_variants(int algo) {
+  return algo == EDPP_SCAN_LOOKBACK ? kLbVariants : algo == EDPP_SCAN_RTS ? kRtsVariants : 0;
+}
+
 }  // namespace edpp
 
 extern "C" {
@@ -712,7 +798,7 @@ int edpp_selftest_lookback_timeout(const int32_t *in, int32_t *out, int64_t leng
   // Tickets start at tile 1: tile 0 is never scanned, so tile 1 (and every
   // later tile) waits for a prefix nobody publishes until the limit runs out.
   return edpp::scan_impl<int32_t, false>(in, out, length, EDPP_SCAN_LOOKBACK, ws, ws_bytes, stream,
-                                         /*tile_base=*/1, timeout_ns);
+                                         /*tile_base=*/1, timeout_ns, /*variant=*/0);
 }
 
 }  // extern "C"

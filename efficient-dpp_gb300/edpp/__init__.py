@@ -83,6 +83,15 @@ SIGNATURES = {
     "edpp_selftest_lookback_timeout": (_I, [_VP, _VP, _I64, _U64, _VP, _SZ, _VP]),
     "edpp_scan_exclusive_i32_noalloc": (_I, [_VP, _VP, _I64, _VP]),
     "edpp_scan_exclusive_i32_noalloc_max_length": (_I64, []),
+    # per-size-class tuning of the plain primitives
+    "edpp_tune_variants": (_I, [_I]),
+    "edpp_tune_set": (_I, [_I, _I, _I, _I, _F]),
+    "edpp_tune_get": (_I, [_I, _I, _I64, _VP]),
+    "edpp_tune_load": (_I, [ctypes.c_char_p]),
+    "edpp_tune_save": (_I, [ctypes.c_char_p]),
+    "edpp_tune_clear": (None, []),
+    "edpp_autotune_plain": (_I, [_I, _VP, _VP, _VP, _I64, _I, _VP, _SZ, _VP, _I, _VP,
+                                 ctypes.POINTER(ctypes.c_float), _VP]),
     # batched segments
     "edpp_batch_plan_create": (_I, [_VP, _I, _VP, ctypes.POINTER(_VP)]),
     "edpp_batch_plan_destroy": (None, [_VP]),
@@ -212,6 +221,48 @@ def _gs(kind, inp, loc, passes, out, method, ws):
     else:
         raise ValueError(method)
     return out
+
+
+# ---------------------------------------------------------------------------
+# per-size-class tuning (include/edpp.h edpp_tune_*)
+TUNE_SCAN_LOOKBACK, TUNE_SCAN_RTS, TUNE_GATHER = 0, 1, 2
+TUNE_NAMES = {TUNE_SCAN_LOOKBACK: "scan_lookback", TUNE_SCAN_RTS: "scan_rts",
+              TUNE_GATHER: "gather"}
+
+
+def tune_get(prim: int, elem_bytes: int, n: int):
+    """(variant a call of n elements takes now, whether the table has an entry)."""
+    v = ctypes.c_int(0)
+    st = lib().edpp_tune_get(prim, elem_bytes, int(n), ctypes.byref(v))
+    return v.value, st == EDPP_OK
+
+
+def tune_set(prim: int, elem_bytes: int, log2_n: int, variant: int, ms: float = 0.0):
+    check(lib().edpp_tune_set(prim, elem_bytes, log2_n, variant, ms), "tune_set")
+
+
+def tune_load(path=None) -> int:
+    """Replace the table from a file (None: the committed default table)."""
+    return lib().edpp_tune_load(None if path is None else str(path).encode())
+
+
+def tune_save(path):
+    check(lib().edpp_tune_save(str(path).encode()), "tune_save")
+
+
+def autotune_plain(prim: int, x, out, ws, loc=None, reps: int = 5):
+    """Time every variant of `prim` at x's length on these arrays, record the
+    fastest in the table; returns (variant, ms, [ms of every variant])."""
+    best = ctypes.c_int(-1)
+    ms = ctypes.c_float(0.0)
+    nv = lib().edpp_tune_variants(prim)
+    each = (ctypes.c_float * max(nv, 1))()
+    elem = x.element_size()
+    check(lib().edpp_autotune_plain(prim, _p(x), _p(out), _p(loc) if loc is not None else None,
+                                    x.numel(), elem, _p(ws), ws.numel(), current_stream_handle(),
+                                    reps, ctypes.byref(best), ctypes.byref(ms), each),
+          "autotune_plain")
+    return best.value, ms.value, [each[i] for i in range(nv)]
 
 
 def gs_workspace_bytes(kind: str, n: int, passes: int, method: str = "partition") -> int:

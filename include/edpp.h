@@ -153,9 +153,10 @@ int edpp_scatter_i32_tiled(const int32_t *in, int32_t *out, int64_t length,
                            const int32_t *loc, int pass, void *ws, size_t ws_bytes,
                            void *stream);
 /* 1 when a gather of `length` elements is faster as the direct single sweep
- * (edpp_gather_i32, pass 1) than in the tiled form on the current device: its
- * source is small enough (about 2.5x L2) to stay largely in L2.  Scatter
- * always favours the tiled form. */
+ * (edpp_gather_i32, pass 1) than in the tiled form on the current device.
+ * The tuning table's choice for this size class when it has one
+ * (EDPP_TUNE_GATHER), else the rule that the source is small enough (about
+ * 2.5x L2) to stay largely in L2.  Scatter always favours the tiled form. */
 int edpp_gather_prefers_direct(int64_t length);
 
 /* ---- global scan -------------------------------------------------------- */
@@ -471,6 +472,56 @@ int edpp_server_wait(edpp_server *server, uint64_t id, double timeout_s,
 int edpp_server_get_stats(edpp_server *server, edpp_server_stats *stats);
 /* Finish all submitted work, stop the scheduler, free everything. */
 void edpp_server_destroy(edpp_server *server);
+
+/* ---- per-size-class tuning of the plain primitives ---------------------- */
+
+/* Choices the primitives read at call time, per primitive, element size and
+ * size class (log2 of the length); a length takes the entry of the nearest
+ * recorded class, else the default (variant 0).  The reference fixes its
+ * tunables per device by hand (R, L, local and grid sizes of scan_chained,
+ * opencl/test/test_scan_global.cpp:87-94); here they are measured.
+ *   EDPP_TUNE_SCAN_LOOKBACK  look-back tile shape (threads x 16-byte chunks):
+ *                            0 128x8 (16 KB), 1 256x8 (32 KB), 2 512x4 (32 KB)
+ *   EDPP_TUNE_SCAN_RTS       slice of the chunked reduce-then-scan (inputs
+ *                            larger than L2): 0 two tiles, 1 one, 2 four
+ *   EDPP_TUNE_GATHER         0 tiled form, 1 direct single sweep (the choice
+ *                            edpp_gather_prefers_direct reports)
+ * The table is read from efficient-dpp_gb300/tuning/plain_gb300.tsv (beside
+ * the library's lib/ directory) on first use; edpp_tune_load replaces it.
+ * All functions here are host-only and thread-safe. */
+typedef enum {
+    EDPP_TUNE_SCAN_LOOKBACK = 0,
+    EDPP_TUNE_SCAN_RTS = 1,
+    EDPP_TUNE_GATHER = 2
+} edpp_tune_primitive;
+
+/* Number of variants of a primitive (0: not tunable). */
+int edpp_tune_variants(int primitive);
+/* Record `variant` (measured at `ms`, informational) for the class. */
+int edpp_tune_set(int primitive, int elem_bytes, int log2_length, int variant, float ms);
+/* The variant a call of `length` elements takes now (EDPP_OK), or the
+ * default with EDPP_EINVAL when the table has no entry for the primitive. */
+int edpp_tune_get(int primitive, int elem_bytes, int64_t length, int *variant);
+/* Replace the table with a file's entries (NULL: the default file); a
+ * missing file leaves the table empty.  Lines: "name elem_bytes log2_length
+ * variant ms", '#' starts a comment. */
+int edpp_tune_load(const char *path);
+/* Write the table to `path` in the same format. */
+int edpp_tune_save(const char *path);
+/* Empty the table (every primitive takes its default). */
+void edpp_tune_clear(void);
+/* The autotuner: times every variant of `primitive` at `length` on the
+ * caller's arrays (scan: `in` / `out` of elem_bytes = 4 (int32) or 8
+ * (int64) elements, exclusive, ws of edpp_scan_workspace_size for its
+ * algorithm; gather: int32 in / out / loc, ws of
+ * edpp_gather_tiled_workspace_size), CUDA events around `reps` calls after
+ * one warm-up each, and records the fastest in the table (*best_variant,
+ * *best_ms; variant_ms, if not NULL, gets every variant's mean ms).
+ * Synchronises `stream`; overwrites out. */
+int edpp_autotune_plain(int primitive, const void *in, void *out, const int32_t *loc,
+                        int64_t length, int elem_bytes, void *ws, size_t ws_bytes,
+                        void *stream, int reps, int *best_variant, float *best_ms,
+                        float *variant_ms);
 
 /* ---- bounded-wait self-test --------------------------------------------- */
 
