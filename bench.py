@@ -791,8 +791,8 @@ def run_autotune_workload(args, rank, world):
     rows = []
     plan = [(edpp.TUNE_SCAN_LOOKBACK, "int32", range(16, 31, 2)),
             (edpp.TUNE_SCAN_LOOKBACK, "int64", range(16, 30, 2)),
-            (edpp.TUNE_SCAN_RTS, "int32", range(25, 31)),
-            (edpp.TUNE_SCAN_RTS, "int64", range(24, 30)),
+            (edpp.TUNE_SCAN_RTS, "int32", range(20, 31)),
+            (edpp.TUNE_SCAN_RTS, "int64", range(20, 30)),
             (edpp.TUNE_GATHER, "int32", (20, 22, 24, 25, 26, 27, 28))]
     for prim, dt, logs in plan:
         for lg in logs:

@@ -213,7 +213,7 @@ template <typename T> __global__ void __launch_bounds__(1024) scan_partials_kern
 // must be initialised; buffers and barriers are the caller's shared memory.
 // `phase` (bit s: parity of bar[s]'s next completion) carries over between
 // calls on the same barriers.
-template <typename T, bool kInclusive, bool kStreamOut = false>
+template <typename T, bool kInclusive, bool kStreamOut = false, bool kLastUse = false>
 __device__ bool scan_tile_run(const T *in, T *out, int64_t n, int64_t t_lo, int64_t t_hi,
                               T &running, T (*buf)[TS<T>::kTile], typename TS<T>::Shared &sh,
                               uint64_t *bar, uint32_t &phase, bool tma, bool vec_out,
@@ -222,8 +222,9 @@ __device__ bool scan_tile_run(const T *in, T *out, int64_t n, int64_t t_lo, int6
   constexpr int kTile = S::kTile;
   auto count_of = [&](int64_t t) { return static_cast<int>(min64(kTile, n - t * kTile)); };
   // Prologue: stage the first tile.
-  uint32_t bulk_cur = stage_tile<T, kTile, kThreads>(buf[0], in + t_lo * kTile, count_of(t_lo), tma,
-                                                     &bar[0]);
+  const uint64_t policy = kLastUse ? l2_policy_evict_first() : 0;
+  uint32_t bulk_cur = stage_tile<T, kTile, kThreads, kLastUse>(buf[0], in + t_lo * kTile,
+                                                               count_of(t_lo), tma, &bar[0], policy);
   for (int64_t t = t_lo; t < t_hi; ++t) {
     const int slot = static_cast<int>((t - t_lo) & 1);
     const int count = count_of(t);
@@ -231,8 +232,9 @@ __device__ bool scan_tile_run(const T *in, T *out, int64_t n, int64_t t_lo, int6
     // barrier of the previous iteration).
     uint32_t bulk_next = 0;
     if (t + 1 < t_hi)
-      bulk_next = stage_tile<T, kTile, kThreads>(buf[slot ^ 1], in + (t + 1) * kTile,
-                                                 count_of(t + 1), tma, &bar[slot ^ 1]);
+      bulk_next = stage_tile<T, kTile, kThreads, kLastUse>(buf[slot ^ 1], in + (t + 1) * kTile,
+                                                           count_of(t + 1), tma, &bar[slot ^ 1],
+                                                           policy);
     if (bulk_cur) {
       if (!mbar_wait_bounded(&bar[slot], (phase >> slot) & 1u, timeout_ns, fault)) return false;
       phase ^= 1u << slot;
@@ -375,11 +377,13 @@ __global__ void __launch_bounds__(kThreads)
 // kSliceTiles is the slice length in tiles, chosen per size class by the
 // tuning table: variant 0 two tiles (the default), variant 1 one tile,
 // variant 2 four tiles (reduced in two rounds of eight 16-byte loads per
-// thread).  The workspace is sized for one-tile slices, the most.
-constexpr int kRtsVariants = 3;
-constexpr int rts_slice_tiles(int variant) { return variant == 1 ? 1 : variant == 2 ? 4 : 2; }
+// thread), variant 3 two tiles with L2 eviction hints (kHint: the reduce's
+// loads evict-last, the second read's bulk copies evict-first), variant 4
+// two tiles also for inputs that fit L2 (instead of the one-launch fused
+// form).  The workspace is sized for one-tile slices, the most.
+constexpr int kRtsVariants = 5;
 
-template <typename T, bool kInclusive, int kSliceTiles>
+template <typename T, bool kInclusive, int kSliceTiles, bool kHint = false>
 __global__ void __launch_bounds__(kThreads, 4)
     rts_chunked_kernel(const T *in, T *out, int64_t n, int64_t chunks, T *sums, unsigned *cnt,
                        unsigned *abort_flag, bool tma, bool vec_out, uint64_t timeout_ns,
@@ -399,6 +403,7 @@ __global__ void __launch_bounds__(kThreads, 4)
     mbar_init(&bar[1], 1);
     fence_mbar_init();
   }
+  const uint64_t keep = kHint ? l2_policy_evict_last() : 0;
   auto reduce_publish = [&](int64_t c) {
     const int64_t lo = min64(n, (c * G + b) * kSliceTiles * kTile);
     const int64_t hi = min64(n, lo + kSliceTiles * kTile);
@@ -414,7 +419,9 @@ __global__ void __launch_bounds__(kThreads, 4)
       for (int r0 = 0; r0 < kV; r0 += kRound) {
         Chunk<T> q[kRound];
 #pragma unroll
-        for (int k = 0; k < kRound; ++k) q[k].raw = __ldcg(p + (r0 + k) * kThreads + tid);
+        for (int k = 0; k < kRound; ++k)
+          q[k].raw = kHint ? ld_v4_policy(p + (r0 + k) * kThreads + tid, keep)
+                           : __ldcg(p + (r0 + k) * kThreads + tid);
 #pragma unroll
         for (int k = 0; k < kRound; ++k)
 #pragma unroll
@@ -486,8 +493,8 @@ __global__ void __launch_bounds__(kThreads, 4)
     const int64_t t_hi = min64(num_tiles, t_lo + kSliceTiles);
     T running = op_add(base, pre);
     if (t_lo < t_hi &&
-        !scan_tile_run<T, kInclusive, true>(in, out, n, t_lo, t_hi, running, buf, sh, bar, phase,
-                                            tma, vec_out, timeout_ns, fault))
+        !scan_tile_run<T, kInclusive, true, kHint>(in, out, n, t_lo, t_hi, running, buf, sh, bar,
+                                                   phase, tma, vec_out, timeout_ns, fault))
       return;
     base = op_add(base, tot);
     __syncthreads();  // s_red is rewritten in the next iteration
@@ -593,7 +600,7 @@ int launch_lookback(const T *in, T *out, int64_t n, char *w, cudaStream_t st, in
 // The chunked reduce-then-scan with slices of kSlice tiles, as one
 // cooperative launch; EDPP_ENOMEM (a fallback signal, nothing launched) when
 // the kernel cannot be resident on this device.
-template <typename T, bool kInclusive, int kSlice>
+template <typename T, bool kInclusive, int kSlice, bool kHint = false>
 int launch_rts_chunked(const T *in, T *out, int64_t n, char *w, cudaStream_t st, bool tma,
                        bool vec_out, uint64_t timeout_ns, unsigned *fault) {
   static int cresident[64];
@@ -604,7 +611,7 @@ int launch_rts_chunked(const T *in, T *out, int64_t n, char *w, cudaStream_t st,
   std::call_once(conce[dev], [dev] {
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &per_sm, rts_chunked_kernel<T, kInclusive, kSlice>, kThreads, 0) != cudaSuccess)
+            &per_sm, rts_chunked_kernel<T, kInclusive, kSlice, kHint>, kThreads, 0) != cudaSuccess)
       per_sm = 0;
     cresident[dev] = per_sm * device_sm_count();
   });
@@ -624,7 +631,7 @@ int launch_rts_chunked(const T *in, T *out, int64_t n, char *w, cudaStream_t st,
   void *args[] = {const_cast<T **>(&in), &out, &n_arg, &chunks_arg, &sums, &cnt, &abort_flag,
                   &tma_arg, &vec_arg, &to_arg, &fault};
   cudaLaunchCooperativeKernel(
-      reinterpret_cast<const void *>(rts_chunked_kernel<T, kInclusive, kSlice>),
+      reinterpret_cast<const void *>(rts_chunked_kernel<T, kInclusive, kSlice, kHint>),
       dim3(static_cast<unsigned>(g)), dim3(kThreads), args, 0, st);
   return launch_status();
 }
@@ -666,7 +673,9 @@ int scan_impl(const T *in, T *out, int64_t n, int algo, void *ws, size_t ws_byte
   chunk_grid<T>(n, blocks, tpb);
   T *partials = reinterpret_cast<T *>(w + kHeader);
   const int64_t per = tpb * TS<T>::kTile;
-  if (algo == EDPP_SCAN_RTS &&
+  if (algo == EDPP_SCAN_RTS && variant < 0)
+    variant = tuned_variant(EDPP_TUNE_SCAN_RTS, sizeof(T), n, 0);
+  if (algo == EDPP_SCAN_RTS && variant != 4 &&
       static_cast<double>(n) * sizeof(T) <= 0.6 * static_cast<double>(device_l2_bytes())) {
     // the input stays in L2 between the reduce and the scan: one launch
     static int resident[64];
@@ -703,9 +712,12 @@ int scan_impl(const T *in, T *out, int64_t n, int algo, void *ws, size_t ws_byte
   if (algo == EDPP_SCAN_RTS) {
     // larger than L2: the chunked one-launch form, which reads each element
     // from DRAM once
-    if (variant < 0) variant = tuned_variant(EDPP_TUNE_SCAN_RTS, sizeof(T), n, 0);
     int s;
     switch (variant) {
+      case 3:
+        s = launch_rts_chunked<T, kInclusive, 2, true>(in, out, n, w, st, tma, vec_out, timeout_ns,
+                                                       fault);
+        break;
       case 1:
         s = launch_rts_chunked<T, kInclusive, 1>(in, out, n, w, st, tma, vec_out, timeout_ns,
                                                  fault);

@@ -286,14 +286,17 @@ template <typename T, int THREADS, int CHUNKS> struct TileScan {
 // (issued by thread 0) and the rest by plain loads.  Returns the number of
 // bytes in flight on `bar` (0 if none); the caller waits on `bar` and then
 // __syncthreads() before reading.
-template <typename T, int kTile, int THREADS>
+// kLastUse: the tile's bytes are read for the last time, so the bulk copy
+// carries an evict-first L2 hint (`policy` from l2_policy_evict_first).
+template <typename T, int kTile, int THREADS, bool kLastUse = false>
 __device__ __forceinline__ uint32_t stage_tile(T *dst, const T *src, int count, bool tma,
-                                               uint64_t *bar) {
+                                               uint64_t *bar, uint64_t policy = 0) {
   uint32_t bulk = 0;
   if (tma) bulk = (static_cast<uint32_t>(count) * sizeof(T)) & ~15u;
   if (threadIdx.x == 0 && bulk) {
     mbar_arrive_expect_tx(bar, bulk);
-    tma_load_1d(dst, src, bulk, bar);
+    if (kLastUse) tma_load_1d_evict_first(dst, src, bulk, bar, policy);
+    else tma_load_1d(dst, src, bulk, bar);
   }
   const int first = static_cast<int>(bulk / sizeof(T));
   if (first < kTile) {

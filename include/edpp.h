@@ -483,7 +483,10 @@ void edpp_server_destroy(edpp_server *server);
  *   EDPP_TUNE_SCAN_LOOKBACK  look-back tile shape (threads x 16-byte chunks):
  *                            0 128x8 (16 KB), 1 256x8 (32 KB), 2 512x4 (32 KB)
  *   EDPP_TUNE_SCAN_RTS       slice of the chunked reduce-then-scan (inputs
- *                            larger than L2): 0 two tiles, 1 one, 2 four
+ *                            larger than 60% of L2): 0 two tiles, 1 one,
+ *                            2 four, 3 two with L2 eviction hints (first read
+ *                            kept, second read demoted), 4 two tiles and the
+ *                            chunked form also below 60% of L2
  *   EDPP_TUNE_GATHER         0 tiled form, 1 direct single sweep (the choice
  *                            edpp_gather_prefers_direct reports)
  * The table is read from efficient-dpp_gb300/tuning/plain_gb300.tsv (beside

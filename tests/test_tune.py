@@ -19,7 +19,7 @@ def lib(edpp):
 
 def test_variant_counts(lib, edpp):
     assert lib.edpp_tune_variants(edpp.TUNE_SCAN_LOOKBACK) == 3
-    assert lib.edpp_tune_variants(edpp.TUNE_SCAN_RTS) == 3
+    assert lib.edpp_tune_variants(edpp.TUNE_SCAN_RTS) == 5
     assert lib.edpp_tune_variants(edpp.TUNE_GATHER) == 2
     assert lib.edpp_tune_variants(7) == 0
 

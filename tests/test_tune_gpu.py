@@ -39,13 +39,14 @@ def test_lookback_shapes(cuda, tuned, dt, variant):
 
 
 @pytest.mark.parametrize("dt", ["int32", "int64"])
-@pytest.mark.parametrize("variant", [0, 1, 2])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4])
 def test_chunked_rts_slices(cuda, tuned, dt, variant):
     edpp = tuned
     torch = cuda
     elem = 4 if dt == "int32" else 8
-    # larger than 60% of L2, so the chunked form runs; ragged end
-    for n in ((1 << 25) + 5, (3 << 24) + 4097):
+    # larger than 60% of L2, so the chunked form runs (variant 4 also below
+    # that, where the others take the one-launch fused form); ragged ends
+    for n in ((1 << 25) + 5, (3 << 24) + 4097, (1 << 20) + 3, 4097, 1):
         edpp.lib().edpp_tune_clear()
         edpp.tune_set(edpp.TUNE_SCAN_RTS, elem, n.bit_length() - 1, variant)
         tdt = torch.int32 if dt == "int32" else torch.int64
