@@ -191,7 +191,8 @@ void edpp_tune_clear(void) {
 
 int edpp_autotune_plain(int primitive, const void *in, void *out, const int32_t *loc,
                         int64_t length, int elem_bytes, void *ws, size_t ws_bytes, void *stream,
-                        int reps, int *best_variant, float *best_ms, float *variant_ms) {
+                        int reps, void *flush, size_t flush_bytes, int *best_variant,
+                        float *best_ms, float *variant_ms) {
   const int nv = edpp::variants_of(primitive);
   if (nv <= 0 || !best_variant || reps < 1 || length <= 0 || !in || !out) return EDPP_EINVAL;
   if (primitive == EDPP_TUNE_GATHER && (!loc || elem_bytes != 4)) return EDPP_EINVAL;
@@ -223,12 +224,19 @@ int edpp_autotune_plain(int primitive, const void *in, void *out, const int32_t 
   float best_t = 0.0f;
   for (int v = 0; v < nv && status == EDPP_OK; ++v) {
     status = run(v);  // warm-up
-    if (status == EDPP_OK && cudaEventRecord(a, st) != cudaSuccess) status = EDPP_ECUDA;
-    for (int r = 0; r < reps && status == EDPP_OK; ++r) status = run(v);
-    if (status == EDPP_OK && cudaEventRecord(b, st) != cudaSuccess) status = EDPP_ECUDA;
-    if (status == EDPP_OK) status = edpp_sync_status(stream, 0);
     float ms = 0.0f;
-    if (status == EDPP_OK && cudaEventElapsedTime(&ms, a, b) != cudaSuccess) status = EDPP_ECUDA;
+    for (int r = 0; r < reps && status == EDPP_OK; ++r) {
+      if (flush && flush_bytes &&
+          cudaMemsetAsync(flush, r & 0xff, flush_bytes, st) != cudaSuccess)
+        status = EDPP_ECUDA;
+      if (status == EDPP_OK && cudaEventRecord(a, st) != cudaSuccess) status = EDPP_ECUDA;
+      if (status == EDPP_OK) status = run(v);
+      if (status == EDPP_OK && cudaEventRecord(b, st) != cudaSuccess) status = EDPP_ECUDA;
+      if (status == EDPP_OK) status = edpp_sync_status(stream, 0);
+      float one = 0.0f;
+      if (status == EDPP_OK && cudaEventElapsedTime(&one, a, b) != cudaSuccess) status = EDPP_ECUDA;
+      ms += one;
+    }
     if (status != EDPP_OK) break;
     ms /= static_cast<float>(reps);
     if (variant_ms) variant_ms[v] = ms;

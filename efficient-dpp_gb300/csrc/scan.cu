@@ -51,11 +51,13 @@ template <typename T> using TS = TileScan<T, kThreads, kChunks>;
 //   variant 1  256 x 8   32 KB tiles,  6 / 4 blocks per SM (half the tiles,
 //              so half the look-backs)
 //   variant 2  512 x 4   32 KB tiles,  6 / 4 blocks per SM
+//   variant 3  512 x 8   64 KB tiles,  3 / 2 blocks per SM (a quarter of the
+//              look-backs)
 // Variant 0's tiles are the smallest; tile state and workspace are sized
 // for them, so every shape fits the same workspace.
 constexpr int kLbThreads = 128;
 constexpr int kLbChunks = 8;
-constexpr int kLbVariants = 3;
+constexpr int kLbVariants = 4;
 template <typename T> using TSL = TileScan<T, kLbThreads, kLbChunks>;
 static_assert(TSL<int32_t>::kTile == TS<int32_t>::kTile && TSL<int64_t>::kTile == TS<int64_t>::kTile,
               "look-back tiles match the other schemes' tiles");
@@ -662,6 +664,9 @@ int scan_impl(const T *in, T *out, int64_t n, int algo, void *ws, size_t ws_byte
                                                             vec_out, timeout_ns, fault);
       case 2:
         return launch_lookback<T, kInclusive, 512, 4, 6, 4>(in, out, n, w, st, tile_base, tma,
+                                                            vec_out, timeout_ns, fault);
+      case 3:
+        return launch_lookback<T, kInclusive, 512, 8, 3, 2>(in, out, n, w, st, tile_base, tma,
                                                             vec_out, timeout_ns, fault);
       default:
         return launch_lookback<T, kInclusive, kLbThreads, kLbChunks, 12, 8>(

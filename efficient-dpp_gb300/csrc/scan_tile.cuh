@@ -176,7 +176,7 @@ template <typename T, int THREADS, int CHUNKS> struct TileScan {
   static constexpr int kTile = THREADS * CHUNKS * E;
   static constexpr int NT = WARPS * CHUNKS;  // warp totals of a tile
   static constexpr int PER = NT / 32;        // warp totals per lane of warp 0
-  static_assert(NT == 32 || NT == 64, "one warp scans the warp totals");
+  static_assert(NT == 32 || NT == 64 || NT == 128, "one warp scans the warp totals");
 
   struct Shared {
     T warp_tot[NT];  // [k*WARPS + w] inclusive total of warp w in row k

@@ -90,7 +90,7 @@ SIGNATURES = {
     "edpp_tune_load": (_I, [ctypes.c_char_p]),
     "edpp_tune_save": (_I, [ctypes.c_char_p]),
     "edpp_tune_clear": (None, []),
-    "edpp_autotune_plain": (_I, [_I, _VP, _VP, _VP, _I64, _I, _VP, _SZ, _VP, _I, _VP,
+    "edpp_autotune_plain": (_I, [_I, _VP, _VP, _VP, _I64, _I, _VP, _SZ, _VP, _I, _VP, _SZ, _VP,
                                  ctypes.POINTER(ctypes.c_float), _VP]),
     # batched segments
     "edpp_batch_plan_create": (_I, [_VP, _I, _VP, ctypes.POINTER(_VP)]),
@@ -250,9 +250,11 @@ def tune_save(path):
     check(lib().edpp_tune_save(str(path).encode()), "tune_save")
 
 
-def autotune_plain(prim: int, x, out, ws, loc=None, reps: int = 5):
+def autotune_plain(prim: int, x, out, ws, loc=None, reps: int = 5, flush=None):
     """Time every variant of `prim` at x's length on these arrays, record the
-    fastest in the table; returns (variant, ms, [ms of every variant])."""
+    fastest in the table; returns (variant, ms, [ms of every variant]).
+    flush: a CUDA tensor larger than L2, overwritten before every timed call
+    (cold-L2 timing); None times back to back (warm)."""
     best = ctypes.c_int(-1)
     ms = ctypes.c_float(0.0)
     nv = lib().edpp_tune_variants(prim)
@@ -260,7 +262,9 @@ def autotune_plain(prim: int, x, out, ws, loc=None, reps: int = 5):
     elem = x.element_size()
     check(lib().edpp_autotune_plain(prim, _p(x), _p(out), _p(loc) if loc is not None else None,
                                     x.numel(), elem, _p(ws), ws.numel(), current_stream_handle(),
-                                    reps, ctypes.byref(best), ctypes.byref(ms), each),
+                                    reps, _p(flush) if flush is not None else None,
+                                    flush.numel() * flush.element_size() if flush is not None else 0,
+                                    ctypes.byref(best), ctypes.byref(ms), each),
           "autotune_plain")
     return best.value, ms.value, [each[i] for i in range(nv)]
 

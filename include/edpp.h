@@ -481,7 +481,8 @@ void edpp_server_destroy(edpp_server *server);
  * tunables per device by hand (R, L, local and grid sizes of scan_chained,
  * opencl/test/test_scan_global.cpp:87-94); here they are measured.
  *   EDPP_TUNE_SCAN_LOOKBACK  look-back tile shape (threads x 16-byte chunks):
- *                            0 128x8 (16 KB), 1 256x8 (32 KB), 2 512x4 (32 KB)
+ *                            0 128x8 (16 KB), 1 256x8 (32 KB), 2 512x4 (32 KB),
+ *                            3 512x8 (64 KB)
  *   EDPP_TUNE_SCAN_RTS       slice of the chunked reduce-then-scan (inputs
  *                            larger than 60% of L2): 0 two tiles, 1 one,
  *                            2 four, 3 two with L2 eviction hints (first read
@@ -517,14 +518,17 @@ void edpp_tune_clear(void);
  * caller's arrays (scan: `in` / `out` of elem_bytes = 4 (int32) or 8
  * (int64) elements, exclusive, ws of edpp_scan_workspace_size for its
  * algorithm; gather: int32 in / out / loc, ws of
- * edpp_gather_tiled_workspace_size), CUDA events around `reps` calls after
- * one warm-up each, and records the fastest in the table (*best_variant,
- * *best_ms; variant_ms, if not NULL, gets every variant's mean ms).
- * Synchronises `stream`; overwrites out. */
+ * edpp_gather_tiled_workspace_size), CUDA events around each of `reps`
+ * calls after one warm-up, and records the fastest in the table
+ * (*best_variant, *best_ms; variant_ms, if not NULL, gets every variant's
+ * mean ms).  With `flush` (a caller buffer of flush_bytes, larger than L2)
+ * the buffer is overwritten before every timed call, outside the timed
+ * span, so variants are timed with the input out of L2, as a first touch
+ * of the data finds it.  Synchronises `stream`; overwrites out and flush. */
 int edpp_autotune_plain(int primitive, const void *in, void *out, const int32_t *loc,
                         int64_t length, int elem_bytes, void *ws, size_t ws_bytes,
-                        void *stream, int reps, int *best_variant, float *best_ms,
-                        float *variant_ms);
+                        void *stream, int reps, void *flush, size_t flush_bytes,
+                        int *best_variant, float *best_ms, float *variant_ms);
 
 /* ---- bounded-wait self-test --------------------------------------------- */
 

@@ -18,7 +18,7 @@ def lib(edpp):
 
 
 def test_variant_counts(lib, edpp):
-    assert lib.edpp_tune_variants(edpp.TUNE_SCAN_LOOKBACK) == 3
+    assert lib.edpp_tune_variants(edpp.TUNE_SCAN_LOOKBACK) == 4
     assert lib.edpp_tune_variants(edpp.TUNE_SCAN_RTS) == 5
     assert lib.edpp_tune_variants(edpp.TUNE_GATHER) == 2
     assert lib.edpp_tune_variants(7) == 0
@@ -36,7 +36,7 @@ def test_set_get_nearest_class(lib, edpp):
     assert edpp.tune_get(edpp.TUNE_SCAN_LOOKBACK, 8, 1 << 20) == (0, False)  # other element size
     assert edpp.tune_get(edpp.TUNE_GATHER, 4, 1 << 20) == (0, False)  # other primitive
     # out-of-range arguments
-    assert lib.edpp_tune_set(edpp.TUNE_SCAN_LOOKBACK, 4, 20, 3, ctypes.c_float(0)) == edpp.EDPP_EINVAL
+    assert lib.edpp_tune_set(edpp.TUNE_SCAN_LOOKBACK, 4, 20, 4, ctypes.c_float(0)) == edpp.EDPP_EINVAL
     assert lib.edpp_tune_set(edpp.TUNE_SCAN_LOOKBACK, 2, 20, 0, ctypes.c_float(0)) == edpp.EDPP_EINVAL
     assert lib.edpp_tune_set(9, 4, 20, 0, ctypes.c_float(0)) == edpp.EDPP_EINVAL
 
@@ -86,11 +86,11 @@ def test_autotune_rejects_bad_arguments(lib, edpp):
     v = ctypes.c_int()
     ms = ctypes.c_float()
     A = lib.edpp_autotune_plain
-    assert A(9, fake, fake, None, 100, 4, fake, 1 << 20, None, 1, ctypes.byref(v),
-             ctypes.byref(ms), None) == edpp.EDPP_EINVAL
-    assert A(edpp.TUNE_GATHER, fake, fake, None, 100, 4, fake, 1 << 20, None, 1, ctypes.byref(v),
-             ctypes.byref(ms), None) == edpp.EDPP_EINVAL  # gather needs loc
-    assert A(edpp.TUNE_SCAN_LOOKBACK, fake, fake, None, 100, 2, fake, 1 << 20, None, 1,
+    assert A(9, fake, fake, None, 100, 4, fake, 1 << 20, None, 1, None, 0,
              ctypes.byref(v), ctypes.byref(ms), None) == edpp.EDPP_EINVAL
-    assert A(edpp.TUNE_SCAN_LOOKBACK, fake, fake, None, 0, 4, fake, 1 << 20, None, 1,
+    assert A(edpp.TUNE_GATHER, fake, fake, None, 100, 4, fake, 1 << 20, None, 1, None, 0,
+             ctypes.byref(v), ctypes.byref(ms), None) == edpp.EDPP_EINVAL  # gather needs loc
+    assert A(edpp.TUNE_SCAN_LOOKBACK, fake, fake, None, 100, 2, fake, 1 << 20, None, 1, None, 0,
+             ctypes.byref(v), ctypes.byref(ms), None) == edpp.EDPP_EINVAL
+    assert A(edpp.TUNE_SCAN_LOOKBACK, fake, fake, None, 0, 4, fake, 1 << 20, None, 1, None, 0,
              ctypes.byref(v), ctypes.byref(ms), None) == edpp.EDPP_EINVAL

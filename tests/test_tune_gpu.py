@@ -22,7 +22,7 @@ def _ref(x, inclusive):
 
 
 @pytest.mark.parametrize("dt", ["int32", "int64"])
-@pytest.mark.parametrize("variant", [0, 1, 2])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
 def test_lookback_shapes(cuda, tuned, dt, variant):
     edpp = tuned
     elem = 4 if dt == "int32" else 8
@@ -82,7 +82,10 @@ def test_autotune_records_a_choice(cuda, tuned):
     y = torch.empty_like(x)
     ws = edpp.workspace(edpp.scan_workspace_bytes(n, "int32", "lookback"), x.device)
     v, ms, each = edpp.autotune_plain(edpp.TUNE_SCAN_LOOKBACK, x, y, ws, reps=3)
-    assert 0 <= v < 3 and ms > 0 and len(each) == 3 and min(each) == ms
+    assert edpp.tune_get(edpp.TUNE_SCAN_LOOKBACK, 4, n) == (v, True)
+    flush = torch.empty(64 << 20, dtype=torch.int32, device="cuda")  # 256 MB > L2
+    v, ms, each = edpp.autotune_plain(edpp.TUNE_SCAN_LOOKBACK, x, y, ws, reps=3, flush=flush)
+    assert 0 <= v < 4 and ms > 0 and len(each) == 4 and min(each) == ms
     assert edpp.tune_get(edpp.TUNE_SCAN_LOOKBACK, 4, n) == (v, True)
     loc = torch.from_numpy(edpp.gen_permutation(n, 2)).cuda()
     gws = edpp.workspace(edpp.gs_workspace_bytes("gather", n, 1, "tiled"), x.device)
