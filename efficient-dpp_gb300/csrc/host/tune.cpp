@@ -221,7 +221,7 @@ int edpp_autotune_plain(int primitive, const void *in, void *out, const int32_t 
     return EDPP_ECUDA;
   }
   int status = EDPP_OK, best = -1;
-  float best_t = 0.0f;
+  float best_t = 0.0f, first_t = 0.0f;
   for (int v = 0; v < nv && status == EDPP_OK; ++v) {
     status = run(v);  // warm-up
     float ms = 0.0f;
@@ -240,6 +240,7 @@ int edpp_autotune_plain(int primitive, const void *in, void *out, const int32_t 
     if (status != EDPP_OK) break;
     ms /= static_cast<float>(reps);
     if (variant_ms) variant_ms[v] = ms;
+    if (v == 0) first_t = ms;
     if (best < 0 || ms < best_t) {
       best = v;
       best_t = ms;
@@ -248,6 +249,15 @@ int edpp_autotune_plain(int primitive, const void *in, void *out, const int32_t 
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   if (status != EDPP_OK) return status;
+  // Another variant replaces the default (variant 0) only when it is more
+  // than 1% faster: smaller margins are within run-to-run spread, and a
+  // variant chosen on noise can lose more than that under other conditions
+  // (the L2-hint scan, 0.4% ahead at 2^28 with L2 flushed, ran 5% behind
+  // when called back to back).
+  if (best > 0 && best_t > 0.99f * first_t) {
+    best = 0;
+    best_t = first_t;
+  }
   *best_variant = best;
   if (best_ms) *best_ms = best_t;
   return edpp_tune_set(primitive, elem_bytes, edpp::class_of(length), best, best_t);

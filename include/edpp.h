@@ -524,7 +524,9 @@ void edpp_tune_clear(void);
  * mean ms).  With `flush` (a caller buffer of flush_bytes, larger than L2)
  * the buffer is overwritten before every timed call, outside the timed
  * span, so variants are timed with the input out of L2, as a first touch
- * of the data finds it.  Synchronises `stream`; overwrites out and flush. */
+ * of the data finds it.  Another variant replaces the default (0) only when
+ * it is more than 1% faster.  Synchronises `stream`; overwrites out and
+ * flush. */
 int edpp_autotune_plain(int primitive, const void *in, void *out, const int32_t *loc,
                         int64_t length, int elem_bytes, void *ws, size_t ws_bytes,
                         void *stream, int reps, void *flush, size_t flush_bytes,
