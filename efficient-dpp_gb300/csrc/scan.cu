@@ -601,7 +601,8 @@ int launch_lookback(const T *in, T *out, int64_t n, char *w, cudaStream_t st, in
 
 // The chunked reduce-then-scan with slices of kSlice tiles, as one
 // cooperative launch; EDPP_ENOMEM (a fallback signal, nothing launched) when
-// the kernel cannot be resident on this device.
+// the kernel cannot be resident on this device or the cooperative launch is
+// refused.
 template <typename T, bool kInclusive, int kSlice, bool kHint = false>
 int launch_rts_chunked(const T *in, T *out, int64_t n, char *w, cudaStream_t st, bool tma,
                        bool vec_out, uint64_t timeout_ns, unsigned *fault) {
@@ -632,9 +633,14 @@ int launch_rts_chunked(const T *in, T *out, int64_t n, char *w, cudaStream_t st,
   uint64_t to_arg = timeout_ns;
   void *args[] = {const_cast<T **>(&in), &out, &n_arg, &chunks_arg, &sums, &cnt, &abort_flag,
                   &tma_arg, &vec_arg, &to_arg, &fault};
-  cudaLaunchCooperativeKernel(
-      reinterpret_cast<const void *>(rts_chunked_kernel<T, kInclusive, kSlice, kHint>),
-      dim3(static_cast<unsigned>(g)), dim3(kThreads), args, 0, st);
+  if (cudaLaunchCooperativeKernel(
+          reinterpret_cast<const void *>(rts_chunked_kernel<T, kInclusive, kSlice, kHint>),
+          dim3(static_cast<unsigned>(g)), dim3(kThreads), args, 0, st) != cudaSuccess) {
+    // the grid could not be made co-resident (another context holds SMs):
+    // clear the launch error and let the caller take the three-launch form
+    cudaGetLastError();
+    return EDPP_ENOMEM;
+  }
   return launch_status();
 }
 
@@ -709,9 +715,9 @@ int scan_impl(const T *in, T *out, int64_t n, int algo, void *ws, size_t ws_byte
                       &tma_arg, &vec_arg, &to_arg, &fault};
       if (cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(rts_fused_kernel<T, kInclusive>),
                                       dim3(static_cast<unsigned>(g)), dim3(kThreads), args, 0,
-                                      st) != cudaSuccess)
+                                      st) == cudaSuccess)
         return launch_status();
-      return launch_status();
+      cudaGetLastError();  // not co-resident: fall through to the other forms
     }
   }
   if (algo == EDPP_SCAN_RTS) {
