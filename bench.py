@@ -97,6 +97,18 @@ def call_launches(name, p, method="tiled"):
     return 5 if name == "gather" else 4  # count, bases, partition, (fetch,) apply
 
 
+def step_config(n, world):
+    """The `config` of the gather/scatter + STREAM step, the same object in
+    both arms (this library and --impl reference)."""
+    workload = ("multipass gather/scatter (2^28 int32, Fisher-Yates seed 2, passes 1,2,4,8,16) "
+                "+ STREAM copy/scale/add/triad (2^28 f32, scalar 3.0)" if n == 1 << 28 else
+                f"multipass gather/scatter (n={n} int32, Fisher-Yates seed 2, passes 1,2,4,8,16) "
+                f"+ STREAM copy/scale/add/triad (n={n} f32, scalar 3.0)")
+    return {"workload": workload, "n": n, "passes": list(PASSES),
+            "parallelism": f"replicas{world}",
+            "l2": "inputs (1 GiB each at 2^28) larger than L2; no flush"}
+
+
 def measured_peak_gbs():
     f = ROOT / "MEASURED_PEAKS.json"
     if f.exists():
@@ -281,12 +293,8 @@ def run_reference(args, rank, world):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32+f32", "data": "synthetic",
-        "config": {"workload": "multipass gather/scatter (2^28 int32, Fisher-Yates seed 2, "
-                               "passes 1,2,4,8,16) + STREAM copy/scale/add/triad "
-                               "(2^28 f32, scalar 3.0)" if n == 1 << 28 else
-                               f"multipass gather/scatter + STREAM at n={n}",
-                   "n": n, "passes": list(PASSES),
-                   "note": "reference CPU path, same arrays and sizes as the GPU arm"},
+        "config": step_config(n, world),
+        "reference_note": "the reference's CPU path on the same arrays and sizes as the GPU arm",
         "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": threads,
                          "kind": "port",
                          "sample": f"the whole step at n=2^{n.bit_length() - 1} (OpenMP ports of "
@@ -1329,11 +1337,7 @@ def main(argv=None):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "int32+f32", "data": "synthetic",
-            "config": {"workload": "multipass gather/scatter (2^28 int32, Fisher-Yates seed 2, "
-                                   "passes 1,2,4,8,16) + STREAM copy/scale/add/triad "
-                                   "(2^28 f32, scalar 3.0)",
-                       "n": n, "passes": list(PASSES), "parallelism": f"replicas{world}",
-                       "l2": "inputs (1 GiB each) larger than L2; no flush"},
+            "config": step_config(n, world),
             "gather_scatter_method": args.method,
             "primitives": primitives,
             "compare": compare,
