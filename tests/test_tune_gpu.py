@@ -26,7 +26,7 @@ def _ref(x, inclusive):
 def test_lookback_shapes(cuda, tuned, dt, variant):
     edpp = tuned
     elem = 4 if dt == "int32" else 8
-    for n in (1, 3, 4095, 4097, 8191, 8193, 65537, (1 << 20) + 3, (1 << 23) + 11):
+    for n in (1, 3, 4095, 4097, 8191, 8193, 65537, (1 << 20) + 3, (1 << 23) + 11, (1 << 26) + 5):
         edpp.lib().edpp_tune_clear()
         edpp.tune_set(edpp.TUNE_SCAN_LOOKBACK, elem, n.bit_length() - 1, variant)
         x = (edpp.gen_uniform_i32(n, 5, -2**31, 2**31 - 1) if dt == "int32"
