@@ -115,9 +115,23 @@ template <int THREADS> struct ScatterCfg {
   static constexpr int kIters = kSeg / 32;     // per lane
 };
 
+// Bucket runs written by bulk copies (KO and KVS_SOA, 3 to kBulkBuckets
+// buckets, 16-byte-aligned outputs): each staging array then holds
+// stage_len(buckets) elements, the tile plus up to 3 spare slots per bucket
+// so that a run's staging start can share its output start's residue mod 4.
+// Measured at 2^28 pairs against the per-element write-out (same process,
+// both builds): 4 / 8 / 16 buckets 9 / 7 / 4% faster; from 32 buckets on,
+// with runs of 256 elements or fewer, 3-14% slower.
+constexpr int kBulkBuckets = 16;
+__host__ __device__ constexpr int stage_len(int buckets, bool bulk) {
+  return kTile + (bulk ? (3 * buckets + 3) / 4 * 4 : 0);
+}
+
 // Dynamic shared memory of the scatter kernel.
-template <int THREADS, int LAYOUT> size_t scatter_smem_bytes(int buckets) {
-  const size_t stage = (LAYOUT == EDPP_KO) ? kTile * 4 : kTile * 8;
+template <int THREADS, int LAYOUT> size_t scatter_smem_bytes(int buckets, bool bulk = false) {
+  const size_t stage = (LAYOUT == EDPP_KO) ? 4 * static_cast<size_t>(stage_len(buckets, bulk))
+                       : (LAYOUT == EDPP_KVS_SOA) ? 8 * static_cast<size_t>(stage_len(buckets, bulk))
+                                                  : kTile * 8;
   return stage + round_up(static_cast<size_t>(ScatterCfg<THREADS>::kWarps) * buckets * 2, 16) +
          2 * static_cast<size_t>(buckets) * 4 +
          static_cast<size_t>(ScatterCfg<THREADS>::kWarps) * std::min(buckets, 256);  // leaders
@@ -129,16 +143,19 @@ __global__ void __launch_bounds__(THREADS, 2)
     split_scatter_kernel(const int32_t *__restrict__ keys_in, int32_t *__restrict__ keys_out,
                          const int32_t *__restrict__ vals_in, int32_t *__restrict__ vals_out,
                          int64_t n, int buckets, int shift, int64_t tiles,
-                         const int32_t *__restrict__ his, bool tma, uint64_t timeout_ns,
-                         unsigned *fault) {
+                         const int32_t *__restrict__ his, bool tma, bool bulk,
+                         uint64_t timeout_ns, unsigned *fault) {
   using C = ScatterCfg<THREADS>;
-  constexpr bool kKV = LAYOUT != EDPP_KO;
   extern __shared__ __align__(128) unsigned char smem[];
-  // Layout: stage (keys[kTile] + vals[kTile], or pairs[kTile]) | cnt16 | toff | gofs
+  // Layout: stage (keys[L] + vals[L] with L = stage_len, or pairs[kTile]) |
+  // cnt16 | toff | gofs | leaders.  `bulk` (KO / SOA only): runs go out by
+  // bulk copies.
+  const int slen = stage_len(buckets, bulk);
   int32_t *s_keys = reinterpret_cast<int32_t *>(smem);
-  int32_t *s_vals = s_keys + kTile;  // SOA only
+  int32_t *s_vals = s_keys + slen;  // SOA only
   int2 *s_pairs = reinterpret_cast<int2 *>(smem);  // AOS only
-  const size_t stage = kKV ? kTile * 8 : kTile * 4;
+  const size_t stage = LAYOUT == EDPP_KO ? 4 * static_cast<size_t>(slen)
+                       : LAYOUT == EDPP_KVS_SOA ? 8 * static_cast<size_t>(slen) : kTile * 8;
   uint16_t *cnt16 = reinterpret_cast<uint16_t *>(smem + stage);
   int32_t *toff = reinterpret_cast<int32_t *>(
       smem + stage + round_up(static_cast<size_t>(C::kWarps) * buckets * 2, 16));
@@ -279,7 +296,7 @@ __global__ void __launch_bounds__(THREADS, 2)
 #pragma unroll 4
     for (int ww = 0; ww < C::kWarps; ++ww) tot += cnt16[ww * buckets + b];
     toff[b] = tot;  // tile count for now
-    my_total += tot;
+    my_total += tot + ((bulk && tot) ? 3 : 0);  // spare slots to align the run
   }
   // Block exclusive scan of my_total.
   __shared__ int32_t s_wsum[32];
@@ -311,23 +328,33 @@ __global__ void __launch_bounds__(THREADS, 2)
       start += c;
     }
   };
+  // With `bulk`, the run's staging start takes the residue mod 4 of its
+  // output start (within its 3 spare slots); each thread keeps its runs
+  // (output start, staging start, count) for the bulk copies below.
+  constexpr int kMaxOwn = 2;  // buckets per thread: 512 threads, up to 1024 buckets
+  int32_t run_dst[kMaxOwn] = {0, 0}, run_src[kMaxOwn] = {0, 0}, run_cnt[kMaxOwn] = {0, 0};
+  auto place = [&](int k, int b, int32_t dst) {
+    const int32_t c = toff[b];
+    const int32_t s = bulk ? run + static_cast<int32_t>((static_cast<uint32_t>(dst) -
+                                                           static_cast<uint32_t>(run)) & 3u)
+                           : run;
+    // First output index of bucket b from this tile, minus its tile slot.
+    gofs[b] = dst - s;
+    warp_slots(b, s);
+    if (k < kMaxOwn) {
+      run_dst[k] = dst;
+      run_src[k] = s;
+      run_cnt[k] = c;
+    }
+    run += c + ((bulk && c) ? 3 : 0);
+  };
 #pragma unroll
   for (int k = 0; k < kHisPre; ++k) {
     const int b = b_lo + k;
-    if (b < b_hi) {
-      const int32_t c = toff[b];
-      // First output index of bucket b from this tile, minus its tile offset.
-      gofs[b] = his_pre[k] - run;
-      warp_slots(b, run);
-      run += c;
-    }
+    if (b < b_hi) place(k, b, his_pre[k]);
   }
-  for (int b = b_lo + kHisPre; b < b_hi; ++b) {
-    const int32_t c = toff[b];
-    gofs[b] = his[static_cast<int64_t>(b) * tiles + t] - run;
-    warp_slots(b, run);
-    run += c;
-  }
+  for (int b = b_lo + kHisPre; b < b_hi; ++b)
+    place(b - b_lo, b, his[static_cast<int64_t>(b) * tiles + t]);
   __syncthreads();
 
   // -- two buckets: each warp's lanes of one bucket hold consecutive output
@@ -369,6 +396,36 @@ __global__ void __launch_bounds__(THREADS, 2)
         if (LAYOUT == EDPP_KVS_SOA) s_vals[s] = vv[it];
       }
     }
+  }
+  if (bulk) {
+    // -- write out: per bucket run, plain stores for the ragged ends and one
+    // bulk copy per array for the 16-byte-aligned middle --
+    fence_proxy_async_smem();  // the re-layout's writes before the copies read them
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kMaxOwn; ++k) {
+      const int32_t c = run_cnt[k];
+      if (k >= b_hi - b_lo || c == 0) continue;
+      const int32_t d = run_dst[k], s = run_src[k];
+      const int32_t head = min(c, static_cast<int32_t>((4u - (static_cast<uint32_t>(d) & 3u)) & 3u));
+      const int32_t body = (c - head) & ~3;
+      for (int i = 0; i < head; ++i) {
+        keys_out[d + i] = s_keys[s + i];
+        if (LAYOUT == EDPP_KVS_SOA) vals_out[d + i] = s_vals[s + i];
+      }
+      if (body) {
+        tma_store_1d(keys_out + d + head, s_keys + s + head, static_cast<uint32_t>(body) * 4u);
+        if (LAYOUT == EDPP_KVS_SOA)
+          tma_store_1d(vals_out + d + head, s_vals + s + head, static_cast<uint32_t>(body) * 4u);
+      }
+      for (int i = head + body; i < c; ++i) {
+        keys_out[d + i] = s_keys[s + i];
+        if (LAYOUT == EDPP_KVS_SOA) vals_out[d + i] = s_vals[s + i];
+      }
+    }
+    tma_store_commit();
+    tma_store_wait_all();  // the copies are complete before the block's shared memory goes
+    return;
   }
   __syncthreads();
 
@@ -420,10 +477,13 @@ int launch_scatter(const int32_t *keys_in, int32_t *keys_out, const int32_t *val
                    const int32_t *his, bool tma, cudaStream_t st) {
   const int s = set_smem_attr<THREADS, LAYOUT>();
   if (s != EDPP_OK) return s;
-  const size_t smem = scatter_smem_bytes<THREADS, LAYOUT>(buckets);
+  const bool bulk = LAYOUT != EDPP_KVS_AOS && buckets > kDirectBuckets &&
+                    buckets <= kBulkBuckets && aligned16(keys_out) &&
+                    (LAYOUT != EDPP_KVS_SOA || aligned16(vals_out));
+  const size_t smem = scatter_smem_bytes<THREADS, LAYOUT>(buckets, bulk);
   split_scatter_kernel<THREADS, LAYOUT><<<static_cast<unsigned>(tiles), THREADS, smem, st>>>(
-      keys_in, keys_out, vals_in, vals_out, n, buckets, shift, tiles, his, tma, kDefaultWaitNs,
-      fault_word());
+      keys_in, keys_out, vals_in, vals_out, n, buckets, shift, tiles, his, tma, bulk,
+      kDefaultWaitNs, fault_word());
   return launch_status();
 }
 
