@@ -42,7 +42,7 @@ constexpr int kOnePassMax = 1024;     // largest bucket count one pass takes
 constexpr int kHistThreads = 512;
 constexpr int kDirectBuckets = 2;  // up to this many buckets the scatter writes from registers
 // Up to this many bucket bits, each lane keeps one bucket's warp count in a
-// register; above, counts live in shared memory behind a leader table.
+// register; above, counts live in shared memory behind a peer table.
 // Measured at 2^28 pairs (same process, both builds): 3 against 5 bits,
 // 2 buckets 1.10 -> 1.00 ms, 4 buckets 1.28 -> 1.22, 32 buckets 1.51 ->
 // 1.42, the others even; 1 bit made 4 and 8 buckets 7-14% slower.
@@ -127,6 +127,13 @@ __host__ __device__ constexpr int stage_len(int buckets, bool bulk) {
   return kTile + (bulk ? (3 * buckets + 3) / 4 * 4 : 0);
 }
 
+// Peer table of the ranking, per warp: from kRegBits + 1 to 8 bucket bits one
+// 32-bit lane mask per bucket (lanes OR themselves in); above 8 bits one
+// leader byte per value of the low 8 bucket bits.
+__host__ __device__ constexpr int peer_table_bytes(int buckets) {
+  return buckets <= 256 ? 4 * buckets : 256;
+}
+
 // Dynamic shared memory of the scatter kernel.
 template <int THREADS, int LAYOUT> size_t scatter_smem_bytes(int buckets, bool bulk = false) {
   const size_t stage = (LAYOUT == EDPP_KO) ? 4 * static_cast<size_t>(stage_len(buckets, bulk))
@@ -134,7 +141,7 @@ template <int THREADS, int LAYOUT> size_t scatter_smem_bytes(int buckets, bool b
                                                   : kTile * 8;
   return stage + round_up(static_cast<size_t>(ScatterCfg<THREADS>::kWarps) * buckets * 2, 16) +
          2 * static_cast<size_t>(buckets) * 4 +
-         static_cast<size_t>(ScatterCfg<THREADS>::kWarps) * std::min(buckets, 256);  // leaders
+         static_cast<size_t>(ScatterCfg<THREADS>::kWarps) * peer_table_bytes(buckets);
 }
 
 // Two blocks per SM (their staging fills shared memory): at most 64 registers.
@@ -148,7 +155,7 @@ __global__ void __launch_bounds__(THREADS, 2)
   using C = ScatterCfg<THREADS>;
   extern __shared__ __align__(128) unsigned char smem[];
   // Layout: stage (keys[L] + vals[L] with L = stage_len, or pairs[kTile]) |
-  // cnt16 | toff | gofs | leaders.  `bulk` (KO / SOA only): runs go out by
+  // cnt16 | toff | gofs | peer tables.  `bulk` (KO / SOA only): runs go out by
   // bulk copies.
   const int slen = stage_len(buckets, bulk);
   int32_t *s_keys = reinterpret_cast<int32_t *>(smem);
@@ -160,7 +167,7 @@ __global__ void __launch_bounds__(THREADS, 2)
   int32_t *toff = reinterpret_cast<int32_t *>(
       smem + stage + round_up(static_cast<size_t>(C::kWarps) * buckets * 2, 16));
   int32_t *gofs = toff + buckets;
-  uint8_t *s_last = reinterpret_cast<uint8_t *>(gofs + buckets);  // [kWarps][min(buckets, 256)]
+  unsigned char *s_peer = reinterpret_cast<unsigned char *>(gofs + buckets);  // [kWarps][table]
   __shared__ alignas(8) uint64_t bar;
 
   const int64_t t = blockIdx.x;
@@ -199,6 +206,9 @@ __global__ void __launch_bounds__(THREADS, 2)
     }
   }
   for (int i = tid; i < C::kWarps * buckets; i += THREADS) cnt16[i] = 0;
+  if (buckets > (1 << kRegBits) && buckets <= 256)  // the lane masks start empty
+    for (int i = tid; i < C::kWarps * buckets; i += THREADS)
+      reinterpret_cast<uint32_t *>(s_peer)[i] = 0u;
   // This thread's buckets for the per-bucket combine below; the first
   // kHisPre of their global run starts (his[b*T + t], one 32-byte sector
   // each) are loaded now, so the round trip overlaps the tile's ranking.
@@ -218,7 +228,8 @@ __global__ void __launch_bounds__(THREADS, 2)
   const unsigned lt = lanemask_lt();
   const int kbits = 31 - __clz(buckets);
   uint16_t *my_cnt = cnt16 + w * buckets;
-  uint8_t *my_last = s_last + w * min(buckets, 256);
+  uint32_t *my_or = reinterpret_cast<uint32_t *>(s_peer) + w * buckets;  // up to 8 bits
+  uint8_t *my_last = s_peer + w * 256;                                  // above 8 bits
   int32_t kk[C::kIters];
   int32_t vv[C::kIters];
   uint32_t rk[(C::kIters + 1) / 2];  // two 16-bit ranks per register
@@ -260,20 +271,30 @@ __global__ void __launch_bounds__(THREADS, 2)
       continue;
     }
     unsigned peers;
-    {
-      // more than 5 bucket bits: the lanes sharing the low 8 bucket bits
-      // agree on one leader lane (whichever write lands), 5 votes on the
-      // leader's lane number find that group, and one vote per bucket bit
-      // above the 8th splits it
+    if (kbits <= 8) {
+      // every lane ORs its bit into its bucket's mask: the mask read back is
+      // the lane's peer group (2^28 pairs against the leader table below:
+      // 32 / 64 / 256 buckets 6 / 5 / 2% faster)
+      if (valid) atomicOr(&my_or[b], 1u << lane);
+      __syncwarp();
+      peers = valid ? my_or[b] : 0u;
+    } else {
+      // the lanes sharing the low 8 bucket bits agree on one leader lane
+      // (whichever write lands), 5 votes on the leader's lane number find
+      // that group, and one vote per bucket bit above the 8th splits it
+      // (a lane-mask table of all buckets would halve the blocks per SM)
       if (valid) my_last[b & 255] = static_cast<uint8_t>(lane);
       __syncwarp();
       peers = match_low_bits(valid ? my_last[b & 255] : 0u, 5, vmask);
-      if (kbits > 8) peers &= match_low_bits(static_cast<unsigned>(b) >> 8, kbits - 8, vmask);
+      peers &= match_low_bits(static_cast<unsigned>(b) >> 8, kbits - 8, vmask);
     }
     const unsigned lower = peers & lt;
     const uint16_t before = valid ? my_cnt[b] : 0;
     __syncwarp();
-    if (valid && lower == 0u) my_cnt[b] = static_cast<uint16_t>(before + __popc(peers));
+    if (valid && lower == 0u) {
+      my_cnt[b] = static_cast<uint16_t>(before + __popc(peers));
+      if (kbits <= 8) my_or[b] = 0u;  // the group's lowest lane empties the mask
+    }
     __syncwarp();
     kk[it] = key;
     vv[it] = val;
