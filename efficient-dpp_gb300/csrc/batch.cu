@@ -66,9 +66,8 @@ union __align__(128) BatchSmem {
     int32_t keys[kTile];
     int32_t vals[kTile];
     uint16_t cnt16[kWarps * kMaxB];
-    int32_t toff[kMaxB];
     int32_t gofs[kMaxB];
-    uint8_t last[kWarps * kMaxB];  // leader lane per (warp, bucket)
+    uint32_t peer[kWarps * kMaxB];  // lanes of each (warp, bucket), ORed in by rank round
   } split;
   struct {
     uint32_t cnt[kMaxB];
@@ -307,7 +306,10 @@ __device__ __forceinline__ void split_tile_task(const DevSeg &seg, int tile, con
       if (b < B) his_pre[j] = __ldcg(his + static_cast<int64_t>(b) * seg.tiles + tile);
     }
   }
-  for (int i = t; i < kWarps * B; i += kThreads) sm.split.cnt16[i] = 0;
+  for (int i = t; i < kWarps * B; i += kThreads) {
+    sm.split.cnt16[i] = 0;
+    sm.split.peer[i] = 0u;
+  }
   if (bulk) {
     if (!mbar_wait_bounded(bar, phase, io.timeout_ns, io.fault)) atomicOr(io.abort_flag, 1u);
     phase ^= 1u;
@@ -326,17 +328,20 @@ __device__ __forceinline__ void split_tile_task(const DevSeg &seg, int tile, con
     const int b = valid ? static_cast<int>(static_cast<unsigned>(key) & mask) : -1;
     const unsigned vmask = __ballot_sync(0xffffffffu, valid);
     unsigned peers;
-    if (kbits <= 5) {
+    if (kbits <= 3) {
       peers = match_low_bits(static_cast<unsigned>(b), kbits, vmask);
-    } else {  // one leader lane per bucket, 5 votes on its lane number
-      if (valid) sm.split.last[w * B + b] = static_cast<uint8_t>(lane);
+    } else {  // each lane ORs its bit into its bucket's mask and reads the group back
+      if (valid) atomicOr(&sm.split.peer[w * B + b], 1u << lane);
       __syncwarp();
-      peers = match_low_bits(valid ? sm.split.last[w * B + b] : 0u, 5, vmask);
+      peers = valid ? sm.split.peer[w * B + b] : 0u;
     }
     const unsigned lower = peers & lt;
     const uint16_t before = valid ? my[b] : 0;
     __syncwarp();
-    if (valid && lower == 0u) my[b] = static_cast<uint16_t>(before + __popc(peers));
+    if (valid && lower == 0u) {
+      my[b] = static_cast<uint16_t>(before + __popc(peers));
+      if (kbits > 3) sm.split.peer[w * B + b] = 0u;
+    }
     __syncwarp();
     kk[it] = key;
     vv[it] = val;
@@ -345,19 +350,16 @@ __device__ __forceinline__ void split_tile_task(const DevSeg &seg, int tile, con
     else rk[it >> 1] = r;
   }
   __syncthreads();
-  // per bucket: exclusive prefix over warps; tile counts; tile offsets
+  // per bucket: tile count, tile offset, then each warp's first slot
+  // (cnt16[w][b] becomes the bucket's tile offset plus the counts of the
+  // warps before w, so the re-layout looks up one counter per element)
   if (t < 32) {
     int32_t run_total = 0;
     for (int b0 = 0; b0 < B; b0 += 32) {
       const int b = b0 + lane;
       int32_t tot = 0;
-      if (b < B) {
-        for (int ww = 0; ww < kWarps; ++ww) {
-          const int32_t c = sm.split.cnt16[ww * B + b];
-          sm.split.cnt16[ww * B + b] = static_cast<uint16_t>(tot);
-          tot += c;
-        }
-      }
+      if (b < B)
+        for (int ww = 0; ww < kWarps; ++ww) tot += sm.split.cnt16[ww * B + b];
       int32_t incl = tot;
 #pragma unroll
       for (int d = 1; d < 32; d <<= 1) {
@@ -366,7 +368,12 @@ __device__ __forceinline__ void split_tile_task(const DevSeg &seg, int tile, con
       }
       if (b < B) {
         const int32_t off = run_total + incl - tot;
-        sm.split.toff[b] = off;
+        int32_t slot = off;
+        for (int ww = 0; ww < kWarps; ++ww) {
+          const int32_t c = sm.split.cnt16[ww * B + b];
+          sm.split.cnt16[ww * B + b] = static_cast<uint16_t>(slot);
+          slot += c;
+        }
         const int j = b0 / 32;
         const int32_t start = j == 0   ? his_pre[0]
                               : j == 1 ? his_pre[1]
@@ -383,7 +390,7 @@ __device__ __forceinline__ void split_tile_task(const DevSeg &seg, int tile, con
     if (pos < count) {
       const int b = static_cast<int>(static_cast<unsigned>(kk[it]) & mask);
       const int r = static_cast<int>((rk[it >> 1] >> ((it & 1) * 16)) & 0xffffu);
-      const int s = sm.split.toff[b] + sm.split.cnt16[w * B + b] + r;
+      const int s = sm.split.cnt16[w * B + b] + r;
       sm.split.keys[s] = kk[it];
       sm.split.vals[s] = vv[it];
     }
