@@ -13,7 +13,8 @@ and compare each result with the oracle's sequential scan and with the
 workspace-taking edpp_scan_exclusive_i32 (LOOKBACK) on the same input.
 Integer scans are compared exactly.  A further test checks the defining
 property: after a warm-up call, calls at the maximum length leave the
-device's free memory unchanged.  This file is named to be collected last.
+device's free memory unchanged; another captures one call in a CUDA graph
+and replays it.  This file is named to be collected last.
 """
 import ctypes
 
@@ -85,6 +86,34 @@ def test_noalloc_leaves_free_memory_unchanged(cuda, edpp, orc):
     total = int(np.sum(h.astype(np.int64))) & 0xFFFFFFFF
     last = (int(out[-1].item()) + int(h[-1])) & 0xFFFFFFFF
     assert out[0].item() == 0 and last == total
+
+
+def test_noalloc_in_cuda_graph(cuda, edpp, orc):
+    # after a warm-up call, one call is captured in a CUDA graph (its look-back
+    # state clear and its kernel); each replay must give the workspace scan's
+    # result again, on fresh input written into the same buffer
+    torch = cuda
+    n = 2_000_003
+    x = torch.from_numpy(edpp.gen_uniform_i32(n, 4, -1000, 1000)).cuda()
+    out = torch.full_like(x, -1)
+    _scan_noalloc(edpp, torch, x, out)  # warm-up outside the capture
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        with torch.cuda.graph(g):
+            _scan_noalloc(edpp, torch, x, out)
+    torch.cuda.current_stream().wait_stream(s)
+    for seed in (5, 6):
+        h = edpp.gen_uniform_i32(n, seed, -1000, 1000)
+        x.copy_(torch.from_numpy(h))
+        out.fill_(-1)
+        g.replay()
+        torch.cuda.synchronize()
+        assert edpp.sync_status() == edpp.EDPP_OK
+        assert np.array_equal(out.cpu().numpy(), orc.scan(h, False)), f"replay with seed {seed}"
+        assert torch.equal(out, _scan_with_workspace(edpp, torch, x))
 
 
 def test_noalloc_limit_and_arguments(cuda, edpp):
