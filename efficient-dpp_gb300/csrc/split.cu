@@ -43,10 +43,10 @@ constexpr int kHistThreads = 512;
 constexpr int kDirectBuckets = 2;  // up to this many buckets the scatter writes from registers
 // Up to this many bucket bits, each lane keeps one bucket's warp count in a
 // register; above, counts live in shared memory behind a peer table.
-// Measured at 2^28 pairs (same process, both builds): 3 against 5 bits,
-// 2 buckets 1.10 -> 1.00 ms, 4 buckets 1.28 -> 1.22, 32 buckets 1.51 ->
-// 1.42, the others even; 1 bit made 4 and 8 buckets 7-14% slower.
-constexpr int kRegBits = 3;
+// Measured at 2^28 pairs (same process, both builds), against the lane-mask
+// table: 2 against 3 bits, 8 buckets 1.27 -> 1.12 ms, the others even; 1
+// bit made 4 buckets 5% slower.
+constexpr int kRegBits = 2;
 
 __device__ __forceinline__ unsigned lanemask_lt() {
   unsigned m;
@@ -145,7 +145,12 @@ template <int THREADS, int LAYOUT> size_t scatter_smem_bytes(int buckets, bool b
 }
 
 // Two blocks per SM (their staging fills shared memory): at most 64 registers.
-template <int THREADS, int LAYOUT>
+// kWide: more than 256 buckets, ranked through the leader table; up to 256
+// buckets the register counts and lane masks.  Two kernels rather than one
+// carrying every form: 16 / 32 / 64 / 256 buckets 19 / 14 / 12 / 7% faster
+// at 2^28 pairs, 512 and 1024 even (one process, both builds).  A third
+// kernel for the register counts alone spilled and made 2 buckets 4% slower.
+template <int THREADS, int LAYOUT, bool kWide>
 __global__ void __launch_bounds__(THREADS, 2)
     split_scatter_kernel(const int32_t *__restrict__ keys_in, int32_t *__restrict__ keys_out,
                          const int32_t *__restrict__ vals_in, int32_t *__restrict__ vals_out,
@@ -206,7 +211,7 @@ __global__ void __launch_bounds__(THREADS, 2)
     }
   }
   for (int i = tid; i < C::kWarps * buckets; i += THREADS) cnt16[i] = 0;
-  if (buckets > (1 << kRegBits) && buckets <= 256)  // the lane masks start empty
+  if (!kWide && buckets > (1 << kRegBits))  // the lane masks start empty
     for (int i = tid; i < C::kWarps * buckets; i += THREADS)
       reinterpret_cast<uint32_t *>(s_peer)[i] = 0u;
   // This thread's buckets for the per-bucket combine below; the first
@@ -254,7 +259,7 @@ __global__ void __launch_bounds__(THREADS, 2)
     }
     const int b = valid ? static_cast<int>((static_cast<unsigned>(key) >> shift) & mask) : -1;
     const unsigned vmask = __ballot_sync(0xffffffffu, valid);
-    if (kbits <= kRegBits) {
+    if (!kWide && kbits <= kRegBits) {
       unsigned peers = vmask, mine = vmask;
       for (int i = 0; i < kbits; ++i) {
         const unsigned bb = __ballot_sync(0xffffffffu, (b >> i) & 1);
@@ -271,10 +276,10 @@ __global__ void __launch_bounds__(THREADS, 2)
       continue;
     }
     unsigned peers;
-    if (kbits <= 8) {
+    if (!kWide) {
       // every lane ORs its bit into its bucket's mask: the mask read back is
-      // the lane's peer group (2^28 pairs against the leader table below:
-      // 32 / 64 / 256 buckets 6 / 5 / 2% faster)
+      // the lane's peer group (2^28 pairs against the leader table below,
+      // in one kernel with it: 32 / 64 / 256 buckets 6 / 5 / 2% faster)
       if (valid) atomicOr(&my_or[b], 1u << lane);
       __syncwarp();
       peers = valid ? my_or[b] : 0u;
@@ -293,7 +298,7 @@ __global__ void __launch_bounds__(THREADS, 2)
     __syncwarp();
     if (valid && lower == 0u) {
       my_cnt[b] = static_cast<uint16_t>(before + __popc(peers));
-      if (kbits <= 8) my_or[b] = 0u;  // the group's lowest lane empties the mask
+      if (!kWide) my_or[b] = 0u;  // the group's lowest lane empties the mask
     }
     __syncwarp();
     kk[it] = key;
@@ -302,7 +307,7 @@ __global__ void __launch_bounds__(THREADS, 2)
     if (it & 1) rk[it >> 1] |= r << 16;
     else rk[it >> 1] = r;
   }
-  if (kbits <= kRegBits && lane < buckets) my_cnt[lane] = static_cast<uint16_t>(lane_cnt);
+  if (!kWide && kbits <= kRegBits && lane < buckets) my_cnt[lane] = static_cast<uint16_t>(lane_cnt);
   __syncthreads();
 
   // -- per bucket: tile count, tile offset, then each warp's first slot --
@@ -383,7 +388,7 @@ __global__ void __launch_bounds__(THREADS, 2)
   // stretches; write from registers, skipping the shared-memory re-layout
   // (2^28 pairs: 1.21 -> 1.11 ms; at 4 buckets even, at 8 and more slower,
   // the stores' sectors being only partly filled) --
-  if (buckets <= kDirectBuckets) {
+  if (!kWide && buckets <= kDirectBuckets) {
 #pragma unroll
     for (int it = 0; it < C::kIters; ++it) {
       const int pos = w * C::kSeg + it * 32 + lane;
@@ -418,7 +423,7 @@ __global__ void __launch_bounds__(THREADS, 2)
       }
     }
   }
-  if (bulk) {
+  if (!kWide && bulk) {
     // -- write out: per bucket run, plain stores for the ragged ends and one
     // bulk copy per array for the 16-byte-aligned middle --
     fence_proxy_async_smem();  // the re-layout's writes before the copies read them
@@ -477,15 +482,15 @@ size_t his_bytes(int64_t tiles, int buckets) {
   return round_up(static_cast<size_t>(tiles) * buckets * 4, 256);
 }
 
-template <int THREADS, int LAYOUT> int set_smem_attr() {
+template <int THREADS, int LAYOUT, bool kWide> int set_smem_attr() {
   static std::once_flag once[64];
   static int status[64];
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64) dev = 0;
   std::call_once(once[dev], [&] {
-    const size_t bytes = scatter_smem_bytes<THREADS, LAYOUT>(kOnePassMax);
-    status[dev] = cuda_status(cudaFuncSetAttribute(split_scatter_kernel<THREADS, LAYOUT>,
+    const size_t bytes = scatter_smem_bytes<THREADS, LAYOUT>(kWide ? kOnePassMax : 256, true);
+    status[dev] = cuda_status(cudaFuncSetAttribute(split_scatter_kernel<THREADS, LAYOUT, kWide>,
                                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                    static_cast<int>(bytes)));
   });
@@ -496,15 +501,22 @@ template <int THREADS, int LAYOUT>
 int launch_scatter(const int32_t *keys_in, int32_t *keys_out, const int32_t *vals_in,
                    int32_t *vals_out, int64_t n, int buckets, int shift, int64_t tiles,
                    const int32_t *his, bool tma, cudaStream_t st) {
-  const int s = set_smem_attr<THREADS, LAYOUT>();
+  const bool wide = buckets > 256;
+  const int s = wide ? set_smem_attr<THREADS, LAYOUT, true>() : set_smem_attr<THREADS, LAYOUT, false>();
   if (s != EDPP_OK) return s;
   const bool bulk = LAYOUT != EDPP_KVS_AOS && buckets > kDirectBuckets &&
                     buckets <= kBulkBuckets && aligned16(keys_out) &&
                     (LAYOUT != EDPP_KVS_SOA || aligned16(vals_out));
   const size_t smem = scatter_smem_bytes<THREADS, LAYOUT>(buckets, bulk);
-  split_scatter_kernel<THREADS, LAYOUT><<<static_cast<unsigned>(tiles), THREADS, smem, st>>>(
-      keys_in, keys_out, vals_in, vals_out, n, buckets, shift, tiles, his, tma, bulk,
-      kDefaultWaitNs, fault_word());
+  const unsigned grid = static_cast<unsigned>(tiles);
+  if (wide)
+    split_scatter_kernel<THREADS, LAYOUT, true><<<grid, THREADS, smem, st>>>(
+        keys_in, keys_out, vals_in, vals_out, n, buckets, shift, tiles, his, tma, bulk,
+        kDefaultWaitNs, fault_word());
+  else
+    split_scatter_kernel<THREADS, LAYOUT, false><<<grid, THREADS, smem, st>>>(
+        keys_in, keys_out, vals_in, vals_out, n, buckets, shift, tiles, his, tma, bulk,
+        kDefaultWaitNs, fault_word());
   return launch_status();
 }
 
