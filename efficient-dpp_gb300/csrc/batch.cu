@@ -277,8 +277,9 @@ __device__ __forceinline__ void hist_tile_task(const DevSeg &seg, int tile, cons
 // 16-byte-aligned part) on `bar`; warp 0 loads the tile's first 64 run
 // starts before the ranking, so that round trip overlaps it.
 constexpr int kHisPre = 2;  // run starts per lane of warp 0 loaded early
-__device__ __forceinline__ void split_tile_task(const DevSeg &seg, int tile, const TaskIO &io,
-                                                BatchSmem &sm, uint64_t *bar, uint32_t &phase) {
+template <bool kMask>
+__device__ __forceinline__ void split_tile_run(const DevSeg &seg, int tile, const TaskIO &io,
+                                               BatchSmem &sm, uint64_t *bar, uint32_t &phase) {
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
   const unsigned lt = lanemask_lt_b();
   const int64_t tile_base = static_cast<int64_t>(tile) * kTile;
@@ -308,7 +309,7 @@ __device__ __forceinline__ void split_tile_task(const DevSeg &seg, int tile, con
   }
   for (int i = t; i < kWarps * B; i += kThreads) {
     sm.split.cnt16[i] = 0;
-    sm.split.peer[i] = 0u;
+    if (kMask) sm.split.peer[i] = 0u;
   }
   if (bulk) {
     if (!mbar_wait_bounded(bar, phase, io.timeout_ns, io.fault)) atomicOr(io.abort_flag, 1u);
@@ -328,7 +329,7 @@ __device__ __forceinline__ void split_tile_task(const DevSeg &seg, int tile, con
     const int b = valid ? static_cast<int>(static_cast<unsigned>(key) & mask) : -1;
     const unsigned vmask = __ballot_sync(0xffffffffu, valid);
     unsigned peers;
-    if (kbits <= 3) {
+    if (!kMask) {
       peers = match_low_bits(static_cast<unsigned>(b), kbits, vmask);
     } else {  // each lane ORs its bit into its bucket's mask and reads the group back
       if (valid) atomicOr(&sm.split.peer[w * B + b], 1u << lane);
@@ -340,7 +341,7 @@ __device__ __forceinline__ void split_tile_task(const DevSeg &seg, int tile, con
     __syncwarp();
     if (valid && lower == 0u) {
       my[b] = static_cast<uint16_t>(before + __popc(peers));
-      if (kbits > 3) sm.split.peer[w * B + b] = 0u;
+      if (kMask) sm.split.peer[w * B + b] = 0u;
     }
     __syncwarp();
     kk[it] = key;
@@ -403,6 +404,14 @@ __device__ __forceinline__ void split_tile_task(const DevSeg &seg, int tile, con
     io.out0[o] = key;
     io.out1[o] = sm.split.vals[s];
   }
+}
+
+// Ranking form chosen once per tile (votes up to 8 buckets, lane masks
+// above), so each form's unrolled loop is compiled on its own.
+__device__ __forceinline__ void split_tile_task(const DevSeg &seg, int tile, const TaskIO &io,
+                                                BatchSmem &sm, uint64_t *bar, uint32_t &phase) {
+  if (seg.buckets > 8) split_tile_run<true>(seg, tile, io, sm, bar, phase);
+  else split_tile_run<false>(seg, tile, io, sm, bar, phase);
 }
 
 // ---- QUEUE schedule: one persistent launch over the work queue ----
