@@ -407,7 +407,10 @@ __global__ void __launch_bounds__(THREADS, 2)
     return;
   }
 
-  // -- re-lay the tile out in bucket order (stable) --
+  // -- re-lay the tile out in bucket order (stable); without bulk copies the
+  // key/value pairs of KVS_SOA are staged interleaved, one 8-byte store per
+  // element (2^28 pairs: 32 to 1024 buckets 2-6% faster than two 4-byte
+  // stores into separate arrays) --
 #pragma unroll
   for (int it = 0; it < C::kIters; ++it) {
     const int pos = w * C::kSeg + it * 32 + lane;
@@ -415,7 +418,7 @@ __global__ void __launch_bounds__(THREADS, 2)
       const int b = static_cast<int>((static_cast<unsigned>(kk[it]) >> shift) & mask);
       const int r = static_cast<int>((rk[it >> 1] >> ((it & 1) * 16)) & 0xffffu);
       const int s = cnt16[w * buckets + b] + r;
-      if (LAYOUT == EDPP_KVS_AOS) {
+      if (LAYOUT == EDPP_KVS_AOS || (LAYOUT == EDPP_KVS_SOA && !bulk)) {
         s_pairs[s] = make_int2(kk[it], vv[it]);
       } else {
         s_keys[s] = kk[it];
@@ -461,6 +464,12 @@ __global__ void __launch_bounds__(THREADS, 2)
       const int2 p = s_pairs[s];
       const int b = static_cast<int>((static_cast<unsigned>(p.x) >> shift) & mask);
       reinterpret_cast<int2 *>(keys_out)[gofs[b] + s] = p;
+    } else if (LAYOUT == EDPP_KVS_SOA) {
+      const int2 p = s_pairs[s];
+      const int b = static_cast<int>((static_cast<unsigned>(p.x) >> shift) & mask);
+      const int64_t o = static_cast<int64_t>(gofs[b]) + s;
+      keys_out[o] = p.x;
+      vals_out[o] = p.y;
     } else {
       const int32_t key = s_keys[s];
       const int b = static_cast<int>((static_cast<unsigned>(key) >> shift) & mask);
