@@ -63,7 +63,7 @@ union __align__(128) BatchSmem {
     TS32::Shared sh;
   } scan;
   struct {
-    int32_t keys[kTile];
+    int32_t keys[kTile];  // with vals: the tile as loaded; re-laid out, {key, value} pairs
     int32_t vals[kTile];
     uint16_t cnt16[kWarps * kMaxB];
     int32_t gofs[kMaxB];
@@ -392,17 +392,17 @@ __device__ __forceinline__ void split_tile_run(const DevSeg &seg, int tile, cons
       const int b = static_cast<int>(static_cast<unsigned>(kk[it]) & mask);
       const int r = static_cast<int>((rk[it >> 1] >> ((it & 1) * 16)) & 0xffffu);
       const int s = sm.split.cnt16[w * B + b] + r;
-      sm.split.keys[s] = kk[it];
-      sm.split.vals[s] = vv[it];
+      reinterpret_cast<int2 *>(sm.split.keys)[s] = make_int2(kk[it], vv[it]);
     }
   }
   __syncthreads();
   for (int s = t; s < count; s += kThreads) {
-    const int32_t key = sm.split.keys[s];
+    const int2 kv = reinterpret_cast<const int2 *>(sm.split.keys)[s];
+    const int32_t key = kv.x;
     const int b = static_cast<int>(static_cast<unsigned>(key) & mask);
     const int64_t o = seg.off + sm.split.gofs[b] + s;
     io.out0[o] = key;
-    io.out1[o] = sm.split.vals[s];
+    io.out1[o] = kv.y;
   }
 }
 
