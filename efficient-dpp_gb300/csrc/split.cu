@@ -238,9 +238,9 @@ __global__ void __launch_bounds__(THREADS, 2)
   int32_t kk[C::kIters];
   int32_t vv[C::kIters];
   uint32_t rk[(C::kIters + 1) / 2];  // two 16-bit ranks per register
-  // Up to 32 buckets: lane L keeps the warp's running count of bucket L in a
-  // register; the per-bit votes give both this lane's group and bucket L's
-  // group, so the loop needs no shared memory and no warp barriers.
+  // Up to 2^kRegBits buckets: lane L keeps the warp's running count of bucket
+  // L in a register; the per-bit votes give both this lane's group and bucket
+  // L's group, so the loop needs no shared memory and no warp barriers.
   uint32_t lane_cnt = 0;
 #pragma unroll
   for (int it = 0; it < C::kIters; ++it) {
