@@ -39,7 +39,7 @@ def test_uniform_keys(cuda, edpp, orc, B, n, layout):
     np.testing.assert_array_equal(st, es)
 
 
-@pytest.mark.parametrize("B", [2, 64, 256, 1024, 2048, 4096, 8192])  # 2048+: two stable passes
+@pytest.mark.parametrize("B", [2, 8, 16, 32, 64, 256, 1024, 2048, 4096, 8192])  # 2048+: two passes
 def test_zipf_keys_large(cuda, edpp, orc, B):
     n = (1 << 22) + 77
     keys = edpp.gen_keys_zipf(n, 3, B, 1.0)
@@ -49,6 +49,31 @@ def test_zipf_keys_large(cuda, edpp, orc, B):
     np.testing.assert_array_equal(ko, ek)
     np.testing.assert_array_equal(vo, ev)
     np.testing.assert_array_equal(st, es)
+
+
+@pytest.mark.parametrize("B", [4, 8, 16, 256, 1024])
+@pytest.mark.parametrize("layout", ["ko", "soa", "aos"])
+def test_one_bucket_holds_every_key(cuda, edpp, orc, B, layout):
+    # every lane of every warp ranks into the same bucket (the ranking's
+    # same-address worst case): the output is the input order and every
+    # bucket starts at 0 (all buckets below the last one are empty)
+    n = 3 * 8192 + 555
+    keys = (edpp.gen_uniform_i32(n, 8, 0, 1 << 20) * B + (B - 1)).astype(np.int32)
+    vals = np.arange(n, dtype=np.int32)
+    if layout == "aos":
+        pairs = np.stack([keys, vals], axis=1)
+        ko, _, st = _run(edpp, pairs, B, "aos")
+        ek, _, es = orc.split(pairs, B, layout="aos")
+        np.testing.assert_array_equal(ko, pairs.reshape(-1) if ko.ndim == 1 else pairs)
+    else:
+        ko, vo, st = _run(edpp, keys, B, layout, vals if layout == "soa" else None)
+        ek, ev, es = orc.split(keys, B, vals if layout == "soa" else None, layout=layout)
+        np.testing.assert_array_equal(ko, keys)
+        if layout == "soa":
+            np.testing.assert_array_equal(vo, vals)
+    np.testing.assert_array_equal(ko, ek)
+    np.testing.assert_array_equal(st, es)
+    assert not st.any()
 
 
 def test_negative_keys_and_unaligned(cuda, edpp, orc):
