@@ -273,7 +273,9 @@ __device__ __forceinline__ void hist_tile_task(const DevSeg &seg, int tile, cons
 
 // Stable key/value scatter of one split tile; the segment's histogram is
 // scanned (his[b*T + t] = first output index of bucket b from tile t).
-// Same ranking as split.cu.  The tile comes in by bulk copies (its
+// Ranks as in split.cu, with 16-bit shared counters per (warp, bucket):
+// votes on the bucket bits up to 8 buckets (kMask false), per-warp lane
+// masks above.  The tile comes in by bulk copies (its
 // 16-byte-aligned part) on `bar`; warp 0 loads the tile's first 64 run
 // starts before the ranking, so that round trip overlaps it.
 constexpr int kHisPre = 2;  // run starts per lane of warp 0 loaded early
