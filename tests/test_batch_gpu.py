@@ -155,3 +155,23 @@ def test_random_segment_tables_every_schedule(cuda, edpp, batch, seed):
         g0, g1 = _mask_unused(segs, to_host(o0), to_host(o1))
         np.testing.assert_array_equal(g0, e0)
         np.testing.assert_array_equal(g1, e1)
+
+
+@pytest.mark.parametrize("buckets", [4, 16, 64, 256])
+def test_split_segments_with_one_bucket(cuda, edpp, batch, buckets):
+    # every key of every split segment falls in the last bucket (the
+    # ranking's same-address case): each segment keeps its input order
+    sizes = [1, 33, 4096, 4097, 20000, 70001]
+    segs = batch.layout(sizes, [1] * len(sizes), buckets=buckets)
+    in0, in1 = batch.gen_inputs(segs, seed=21)
+    in0 = (in0 * buckets + (buckets - 1)).astype(np.int32)
+    e0, e1 = reference_outputs(segs, in0, in1)
+    for s in segs:
+        o, L = int(s["offset"]), int(s["length"])
+        np.testing.assert_array_equal(e0[o:o + L], in0[o:o + L])
+    for tu in (None, batch.Tuning(3, 4, 1, 1)):
+        o0, o1, _ = _run_batch(batch, cuda, segs, in0, in1, tu)
+        assert edpp.sync_status() == edpp.EDPP_OK
+        g0, g1 = _mask_unused(segs, to_host(o0), to_host(o1))
+        np.testing.assert_array_equal(g0, _mask_unused(segs, e0, e1)[0])
+        np.testing.assert_array_equal(g1, _mask_unused(segs, e0, e1)[1])
