@@ -433,7 +433,7 @@ def measure_batch(args, dev, world, steps, warmup, autotune=False):
         "launches_per_batch": launches,
         "clocks": clk.summary(),
         "cpu_baseline": None,
-        "cpu_baseline_note": "the comparison north_star names is plain per-segment C-ABI calls "
+        "cpu_baseline_note": "the batched form is compared with plain per-segment C-ABI calls "
                              "on the same GPU (plain.ms)",
     }
 
