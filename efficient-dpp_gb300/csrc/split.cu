@@ -16,9 +16,11 @@
 //              index of bucket b's elements from tile t.
 //  3. scatter: one block per tile stages the tile in shared memory by TMA
 //              bulk copy; every warp ranks its contiguous 1/WARPS of the tile
-//              in input order (peer group from one vote per bucket bit, rank = popc
-//              of lower peers + the warp's running count of the bucket, kept
-//              as 16-bit counters in shared memory); ranks of all warps are
+//              in input order (rank = popc of the lower lanes in the
+//              element's peer group + the warp's running count of the
+//              bucket; the peer group from votes on the bucket bits up to 4
+//              buckets, from a per-warp lane mask per bucket up to 256, from
+//              a leader table plus votes above); ranks of all warps are
 //              combined per bucket, the tile is re-laid out in shared memory
 //              in bucket order, and written out as one contiguous run per
 //              bucket (coalesced), at his[b*T + t] + rank.
